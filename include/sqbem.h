@@ -1,0 +1,150 @@
+/* sqbem.h -- C ABI of the GB300 boundary-element library for a squirmer in a
+ * closed tube (drop-in for the hot path of squirmer-bem-3dtube).
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Arrays are HOST memory unless an entry
+ *     point says otherwise; the library copies them to and from the GPU.
+ *   - A panel is given by its three vertices: V[9*p + 3*k + c] = coordinate c of
+ *     vertex k of panel p.  Normals follow from the vertex order (out of the
+ *     fluid), exactly as Mesh::geometry does in the reference
+ *     (src/utils/mesh.hpp:61-72).
+ *   - Vectors per panel or per point are packed xyz: v[3*p + c].
+ *   - Every call returns an int status (SQBEM_OK = 0).  sqbem_last_error()
+ *     gives the message of the last failure on the calling thread; the C++
+ *     headers rethrow it as std::runtime_error with the reference's wording
+ *     ("dgetrf failed", "dgesv failed", ...).
+ *   - Handles own their device memory and are bound to one CUDA stream.  Calls
+ *     on distinct handles may run on different host threads.
+ *   - There is no CPU fallback: without a CUDA device, compute entry points
+ *     return SQBEM_ERR_NO_DEVICE.
+ */
+#ifndef SQBEM_H
+#define SQBEM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define SQBEM_OK 0
+#define SQBEM_ERR_ARG 1           /* bad argument or size                       */
+#define SQBEM_ERR_SINGULAR 2      /* zero pivot (reference: "dgetrf failed")    */
+#define SQBEM_ERR_CUDA 3          /* CUDA runtime error                         */
+#define SQBEM_ERR_NOT_CONVERGED 4 /* mixed-precision refinement did not reach
+                                     its tolerance within its iteration cap     */
+#define SQBEM_ERR_NO_DEVICE 5     /* no CUDA device                             */
+#define SQBEM_ERR_ALLOC 6         /* device allocation failed                   */
+#define SQBEM_ERR_TIMEOUT 7       /* a bounded device wait gave up              */
+
+/* precision modes */
+#define SQBEM_FP64 0  /* FP64 assembly and FP64 LU/TRSM/GEMM (matches the FP64
+                         reference to 1e-10 relative)                           */
+#define SQBEM_MIXED 1 /* FP32 assembly (FP64 self panels), split-BF16 tensor-core
+                         LU/TRSM/GEMM accumulated in FP32, FP64 refinement      */
+
+/* Message of the last failure on this thread ("" if none). */
+const char* sqbem_last_error(void);
+/* Library version string. */
+const char* sqbem_version(void);
+/* Number of kernel launches issued by this process so far (all entry points). */
+long long sqbem_launch_count(void);
+
+/* ---------------------------------------------------------------- geometry
+ * Host-side mesh generators; the output is bit-identical to the reference.
+ * Each returns the panel count in *P.  V (9 per panel) and tags (1 per panel)
+ * are written only when non-NULL and cap >= *P. */
+
+/* tube_mesh, src/utils/mesh.hpp:149-190 (z: nz1 axial nodes) */
+int sqbem_tube_mesh(double R, const double* z, int nz1, int n_theta, int n_r, double* V, int* tags,
+                    int cap, int* P);
+/* swimmer_tube_mesh, src/utils/mesh.hpp:194-197 */
+int sqbem_swimmer_tube_mesh(double R, double L, double a, int n_theta, int n_r, double* V, int* tags,
+                            int cap, int* P);
+/* uniform_z, src/utils/mesh.hpp:112-116 (nz + 1 nodes into z) */
+int sqbem_uniform_z(double z0, double z1, int nz, double* z);
+/* icosphere, src/utils/mesh.hpp:208-245 (center: 3 doubles) */
+int sqbem_icosphere(double a, int level, const double* center, int tag, double* V, int* tags, int cap,
+                    int* P);
+/* Mesh::geometry, src/utils/mesh.hpp:61-72: per-panel normal (3), centroid (3),
+ * area and h = sqrt(2 area); any output may be NULL. */
+int sqbem_geometry(int P, const double* V, double* normal, double* centroid, double* area, double* h);
+
+/* ---------------------------------------------------------------- quadrature
+ * panel_integrals, src/utils/kernels.hpp:67-82, batched on the GPU: for each of
+ * n (panel, target, self) triples, SL (9, row-major) = int_p G dS and
+ * DL (9) = int_p T.m dS with the reference's adaptive rule (7/28/112/448 points
+ * by distance / panel size, Duffy self integral).  FP64. */
+int sqbem_panel_integrals(int n, const double* V9, const double* x0, const int* self, double* SL,
+                          double* DL);
+
+/* ---------------------------------------------------------------- dense
+ * solve_dense, src/utils/linalg.hpp:53-58 (dgesv) with LUFactor semantics
+ * (linalg.hpp:62-78): B (n x nrhs, column-major) <- A^{-1} B for A (n x n,
+ * column-major), FP64 on the GPU.  *pivoted (may be NULL) reports whether row
+ * exchanges were needed.  A zero pivot returns SQBEM_ERR_SINGULAR with the
+ * message "dgesv failed". */
+int sqbem_solve_dense(int n, int nrhs, const double* A, double* B, int* pivoted);
+
+/* ---------------------------------------------------------------- field
+ * velocity_at, src/utils/field.hpp:18-34: lab-frame velocity at npts points
+ * from the boundary solution (u, f per panel) on the P panels V. */
+int sqbem_velocity_at(int P, const double* V, const double* u, const double* f, double mu, int npts,
+                      const double* pts, double* out, int precision);
+
+/* ---------------------------------------------------------------- tube
+ * Tube, src/swimmer.hpp:33-75: swimmer_tube_mesh + assembly of the tube-tube
+ * single-layer block T (3Nt x 3Nt) + Wielandt deflation + LU, all on the GPU.
+ * The factor stays in device memory for the handle's lifetime. */
+typedef struct sqbem_tube sqbem_tube;
+int sqbem_tube_create(double R, double L, double a, int n_theta, int n_r, double mu, int precision,
+                      sqbem_tube** out);
+/* panel count Nt */
+int sqbem_tube_panels(const sqbem_tube* t, int* Nt);
+/* tube panels (9 doubles each) and tags (Nt each), host arrays */
+int sqbem_tube_mesh_get(const sqbem_tube* t, double* V, int* tags);
+void sqbem_tube_destroy(sqbem_tube* t);
+
+/* ---------------------------------------------------------------- swimmer
+ * SwimmerSolver, src/swimmer.hpp:83-289.  create = constructor + build()
+ * (swimmer.hpp:92-97, 180-251): sphere-tube and sphere-sphere blocks, completed
+ * double layer, deflation, rigid-body map and the Schur complement onto the
+ * sphere tractions and (U, Omega).  tube == NULL is the unbounded fluid.
+ * The tube must outlive the swimmer (non-owning, as in the reference). */
+typedef struct sqbem_swimmer sqbem_swimmer;
+int sqbem_swimmer_create(const sqbem_tube* tube, int Ns, const double* V, const int* tags,
+                         const double* center, double mu, int precision, sqbem_swimmer** out);
+/* solve_free, swimmer.hpp:107-139: force- and torque-free swimming for nrhs slip
+ * fields (slips: nrhs x Ns x 3).  Outputs per right-hand side k: U[3k..],
+ * Om[3k..], f_sphere[k*3Ns..], f_tube[k*3Nt..] (the last two may be NULL). */
+int sqbem_swimmer_solve_free(sqbem_swimmer* s, int nrhs, const double* slips, double* U, double* Om,
+                             double* f_sphere, double* f_tube);
+/* solve_prescribed, swimmer.hpp:142-153: rigid sphere with given U, Omega. */
+int sqbem_swimmer_solve_prescribed(sqbem_swimmer* s, const double* U, const double* Om,
+                                   double* f_sphere, double* f_tube);
+/* t_assembly and t_schur, swimmer.hpp:90 (seconds, device-timed) */
+int sqbem_swimmer_timings(const sqbem_swimmer* s, double* t_assembly, double* t_schur);
+/* refinement diagnostics of the last mixed-precision solve: iterations used and
+ * the final relative FP64 residual (max over right-hand sides) */
+int sqbem_swimmer_refinement(const sqbem_swimmer* s, int* iterations, double* residual);
+void sqbem_swimmer_destroy(sqbem_swimmer* s);
+
+/* ---------------------------------------------------------------- duct flow
+ * DuctFlow, src/duct_flow.hpp:22-109: mixed-BC completed BIE on a closed tube
+ * (tube_mesh(R, uniform_z(0, L, n_z), n_theta, n_r)), LU once, one solve per
+ * pressure drop. */
+typedef struct sqbem_duct sqbem_duct;
+int sqbem_duct_create(double R, double L, int n_theta, int n_z, int n_r, double mu, int precision,
+                      sqbem_duct** out);
+int sqbem_duct_panels(const sqbem_duct* d, int* P);
+int sqbem_duct_mesh_get(const sqbem_duct* d, double* V, int* tags);
+/* DuctFlow::solve, duct_flow.hpp:41-63: u, f (3 per panel, may be NULL), Q */
+int sqbem_duct_solve(sqbem_duct* d, double p_in, double p_out, double* u, double* f, double* Q);
+void sqbem_duct_destroy(sqbem_duct* d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SQBEM_H */

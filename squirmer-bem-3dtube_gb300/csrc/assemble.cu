@@ -1,0 +1,546 @@
+// assemble.cu -- panel-quadrature assembly of the BEM blocks, panel integrals
+// and the field (representation formula) on the GPU.
+//
+// Physics, as in the reference (src/utils/kernels.hpp:8-21, 29-82):
+//   SL_ij = int_p G_ij dS,  G_ij(r) = d_ij/|r| + r_i r_j/|r|^3,
+//   DL_ij = int_p T_ijk m_k dS,  T_ijk(r) = -6 r_i r_j r_k/|r|^5,  r = x - x0,
+// with the rule chosen by d = |c_p - x0| / h_p: d >= 3 -> 7 points, >= 1.5 ->
+// 28, >= 0.75 -> 112, else 448 (Dunavant-7 on 1/4/16/64 sub-triangles), and the
+// self panel by a Duffy transform over three sub-triangles with 10 x 10
+// Gauss-Legendre points (DL = 0 there, since r.m = 0 on a flat panel).
+//
+// GPU structure (one block = a set of target centroids x sources panels):
+//   far_kernel   one thread per (target, source) pair, 64 targets x 16 sources
+//                per CTA; source panels staged in shared memory; pairs with
+//                d >= 3 use the 7-point rule in registers and write their 3x3
+//                blocks (coalesced: consecutive threads own consecutive rows of
+//                a column-major block); pairs with d < 3 and the self pair are
+//                appended to a near list.
+//   near_kernel  one warp per near pair: the lanes split the 28/112/448 rule
+//                points (or the 300 Duffy points), reduce with warp shuffles,
+//                and lanes 0..8 write the entries.  Entries have fixed positions,
+//                so the result does not depend on the list order.
+//   rowsum / completion kernels: the completed double layer adds -sum_p D_ip to
+//                the diagonal 3x3 blocks (duct_flow.hpp:103-105,
+//                swimmer.hpp:218-220), computed by a fixed-order reduction over
+//                the stored D block (deterministic).
+// Precision: FP64 everywhere in SQBEM_FP64 mode.  In SQBEM_MIXED mode the
+// relative vectors e_k = V_k - x0 and the rule choice are FP64, the far (7) and
+// near (28/112) rules are evaluated in FP32 from those accurate vectors, and the
+// 448-point near-singular rule and the Duffy self integrals stay FP64.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "assemble.cuh"
+#include "bem/utils/quadrature.hpp"
+#include "common.cuh"
+
+namespace sqbem {
+
+// ---------------------------------------------------------------- tables
+struct QPoint {
+    double l0, l1, l2, w;
+};
+struct QPointF {
+    float l0, l1, l2, w;
+};
+__host__ __device__ constexpr int rule_off(int r) { return r <= 0 ? 0 : r == 1 ? 7 : r == 2 ? 35 : r == 3 ? 147 : 595; }
+__device__ QPoint d_rule[595];
+__device__ QPointF d_rulef[595];
+__constant__ QPoint c_rule7[7];
+__constant__ QPointF c_rule7f[7];
+__device__ double d_gl_x[10], d_gl_w[10];
+__device__ QPoint d_duffy[100];  // (x_a, x_b, w_a * w_b) for the 10 x 10 GL grid
+
+static std::once_flag g_table_once[64];
+
+void init_tables() {
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) fail(SQBEM_ERR_ARG, "device ordinal %d out of range", dev);
+    std::call_once(g_table_once[dev], [] {
+        std::vector<QPoint> h;
+        std::vector<QPointF> hf;
+        for (const auto& R : bem::rules())
+            for (size_t q = 0; q < R.W.size(); ++q) {
+                h.push_back({R.L[q][0], R.L[q][1], R.L[q][2], R.W[q]});
+                hf.push_back({(float)R.L[q][0], (float)R.L[q][1], (float)R.L[q][2], (float)R.W[q]});
+            }
+        if (h.size() != 595) fail(SQBEM_ERR_ARG, "quadrature table has %zu points", h.size());
+        CUDA_CHECK(cudaMemcpyToSymbol(d_rule, h.data(), sizeof(QPoint) * 595));
+        CUDA_CHECK(cudaMemcpyToSymbol(d_rulef, hf.data(), sizeof(QPointF) * 595));
+        CUDA_CHECK(cudaMemcpyToSymbol(c_rule7, h.data(), sizeof(QPoint) * 7));
+        CUDA_CHECK(cudaMemcpyToSymbol(c_rule7f, hf.data(), sizeof(QPointF) * 7));
+        std::vector<double> gx, gw;
+        bem::gauss_legendre01(10, gx, gw);
+        CUDA_CHECK(cudaMemcpyToSymbol(d_gl_x, gx.data(), sizeof(double) * 10));
+        CUDA_CHECK(cudaMemcpyToSymbol(d_gl_w, gw.data(), sizeof(double) * 10));
+        std::vector<QPoint> duf;
+        for (int a = 0; a < 10; ++a)
+            for (int b = 0; b < 10; ++b) duf.push_back({gx[a], gx[b], 0.0, gw[a] * gw[b]});
+        CUDA_CHECK(cudaMemcpyToSymbol(d_duffy, duf.data(), sizeof(QPoint) * 100));
+        CUDA_CHECK(cudaDeviceSynchronize());
+    });
+}
+
+// ---------------------------------------------------------------- kernel sums
+// Unique entries of the two symmetric 3x3 results plus the 1/|r| diagonal term.
+template <class T>
+struct Acc {
+    T dg, sxx, sxy, sxz, syy, syz, szz, dxx, dxy, dxz, dyy, dyz, dzz;
+    __device__ void zero() { dg = sxx = sxy = sxz = syy = syz = szz = dxx = dxy = dxz = dyy = dyz = dzz = T(0); }
+};
+
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+
+// One quadrature node: accumulate w G(r) and w T(r).m (kernels.hpp:29-40).
+template <class T, bool WITH_DL>
+__device__ __forceinline__ void accum(Acc<T>& A, T rx, T ry, T rz, T w, T mx, T my, T mz) {
+    const T r2 = rx * rx + ry * ry + rz * rz;
+    const T ir = rsqrt_t(r2);
+    const T ir2 = ir * ir;
+    const T ir3 = ir * ir2;
+    const T s = w * ir3;
+    A.dg += w * ir;
+    const T sx = s * rx, sy = s * ry, sz = s * rz;
+    A.sxx += sx * rx; A.sxy += sx * ry; A.sxz += sx * rz;
+    A.syy += sy * ry; A.syz += sy * rz; A.szz += sz * rz;
+    if (WITH_DL) {
+        const T d = T(-6) * w * (rx * mx + ry * my + rz * mz) * ir3 * ir2;
+        const T dx = d * rx, dy = d * ry, dz = d * rz;
+        A.dxx += dx * rx; A.dxy += dx * ry; A.dxz += dx * rz;
+        A.dyy += dy * ry; A.dyz += dy * rz; A.dzz += dz * rz;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void warp_reduce(Acc<T>& A) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        A.dg += __shfl_xor_sync(0xffffffffu, A.dg, o);
+        A.sxx += __shfl_xor_sync(0xffffffffu, A.sxx, o);
+        A.sxy += __shfl_xor_sync(0xffffffffu, A.sxy, o);
+        A.sxz += __shfl_xor_sync(0xffffffffu, A.sxz, o);
+        A.syy += __shfl_xor_sync(0xffffffffu, A.syy, o);
+        A.syz += __shfl_xor_sync(0xffffffffu, A.syz, o);
+        A.szz += __shfl_xor_sync(0xffffffffu, A.szz, o);
+        A.dxx += __shfl_xor_sync(0xffffffffu, A.dxx, o);
+        A.dxy += __shfl_xor_sync(0xffffffffu, A.dxy, o);
+        A.dxz += __shfl_xor_sync(0xffffffffu, A.dxz, o);
+        A.dyy += __shfl_xor_sync(0xffffffffu, A.dyy, o);
+        A.dyz += __shfl_xor_sync(0xffffffffu, A.dyz, o);
+        A.dzz += __shfl_xor_sync(0xffffffffu, A.dzz, o);
+    }
+}
+
+// entry (a, b) of SL or DL from the accumulator
+template <class T>
+__device__ __forceinline__ T sl_entry(const Acc<T>& A, int a, int b) {
+    const int k = a * 3 + b;
+    T v = k == 0 ? A.sxx : k == 1 || k == 3 ? A.sxy : k == 2 || k == 6 ? A.sxz
+        : k == 4 ? A.syy : k == 5 || k == 7 ? A.syz : A.szz;
+    return a == b ? v + A.dg : v;
+}
+template <class T>
+__device__ __forceinline__ T dl_entry(const Acc<T>& A, int a, int b) {
+    const int k = a * 3 + b;
+    return k == 0 ? A.dxx : k == 1 || k == 3 ? A.dxy : k == 2 || k == 6 ? A.dxz
+         : k == 4 ? A.dyy : k == 5 || k == 7 ? A.dyz : A.dzz;
+}
+
+// Rule index of kernels.hpp:74-75 evaluated exactly as the reference does:
+// d = |c - x0| / h with round-to-nearest products and sums in the reference's
+// order (no FMA contraction), IEEE sqrt and division -- so a pair sitting on a
+// threshold picks the same rule.
+__device__ __forceinline__ int rule_of(const PanelRec& P, double x, double y, double z) {
+    const double dx = P.c[0] - x, dy = P.c[1] - y, dz = P.c[2] - z;
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double d = __ddiv_rn(__dsqrt_rn(d2), P.h);
+    return d < 0.75 ? 3 : (d < 1.5 ? 2 : (d < 3.0 ? 1 : 0));
+}
+
+// ---------------------------------------------------------------- whole-pair integrals
+// Sum over one rule's points split across the 32 lanes of a warp (after the
+// call every lane holds the complete sums).  FP64 or FP32 evaluation from the
+// FP64 relative vertex vectors e_k = V_k - x0.
+template <class T>
+__device__ void warp_rule(Acc<T>& A, const PanelRec& P, double x, double y, double z, int rule, int lane) {
+    A.zero();
+    const T e0x = (T)(P.v[0] - x), e0y = (T)(P.v[1] - y), e0z = (T)(P.v[2] - z);
+    const T e1x = (T)(P.v[3] - x), e1y = (T)(P.v[4] - y), e1z = (T)(P.v[5] - z);
+    const T e2x = (T)(P.v[6] - x), e2y = (T)(P.v[7] - y), e2z = (T)(P.v[8] - z);
+    const T mx = (T)P.n[0], my = (T)P.n[1], mz = (T)P.n[2];
+    const T area = (T)P.area;
+    const int q0 = rule_off(rule), q1 = rule_off(rule + 1);
+    for (int q = q0 + lane; q < q1; q += 32) {
+        T l0, l1, l2, w;
+        if constexpr (sizeof(T) == 8) {
+            const QPoint Q = d_rule[q];
+            l0 = Q.l0; l1 = Q.l1; l2 = Q.l2; w = Q.w;
+        } else {
+            const QPointF Q = d_rulef[q];
+            l0 = Q.l0; l1 = Q.l1; l2 = Q.l2; w = Q.w;
+        }
+        const T rx = l0 * e0x + l1 * e1x + l2 * e2x;
+        const T ry = l0 * e0y + l1 * e1y + l2 * e2y;
+        const T rz = l0 * e0z + l1 * e1z + l2 * e2z;
+        accum<T, true>(A, rx, ry, rz, w * area, mx, my, mz);
+    }
+    warp_reduce(A);
+}
+
+// Duffy self integral (kernels.hpp:50-65): x0 inside the panel; three
+// sub-triangles (x0, V_e, V_e+1), x = x0 + u[(1 - v) e1 + v e2], Jacobian u J.
+__device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y, double z, int lane) {
+    A.zero();
+    for (int t = lane; t < 300; t += 32) {
+        const int e = t / 100, g = t % 100;
+        const int f = e == 2 ? 0 : e + 1;
+        const double e1x = P.v[3 * e] - x, e1y = P.v[3 * e + 1] - y, e1z = P.v[3 * e + 2] - z;
+        const double e2x = P.v[3 * f] - x, e2y = P.v[3 * f + 1] - y, e2z = P.v[3 * f + 2] - z;
+        const double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+        const double J = sqrt(cx * cx + cy * cy + cz * cz);
+        const QPoint Q = d_duffy[g];
+        const double u = Q.l0, v = Q.l1;
+        const double rx = u * ((1 - v) * e1x + v * e2x);
+        const double ry = u * ((1 - v) * e1y + v * e2y);
+        const double rz = u * ((1 - v) * e1z + v * e2z);
+        accum<double, false>(A, rx, ry, rz, Q.w * u * J, 0.0, 0.0, 0.0);
+    }
+    warp_reduce(A);
+}
+
+// ---------------------------------------------------------------- far kernel
+constexpr int FAR_TGT = 64;   // targets per CTA (threads)
+constexpr int FAR_SRC = 16;   // source panels per CTA
+
+template <class TO, class TC>
+__global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
+    __shared__ PanelRec sp[FAR_SRC];
+    const int p0 = blockIdx.y * FAR_SRC;
+    const int ns = min(FAR_SRC, job.nS - p0);
+    {
+        const double* src = reinterpret_cast<const double*>(job.src + p0);
+        double* dst = reinterpret_cast<double*>(sp);
+        const int nd = ns * (int)(sizeof(PanelRec) / sizeof(double));
+        for (int k = threadIdx.x; k < nd; k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    const int i = blockIdx.x * FAR_TGT + threadIdx.x;
+    if (i >= job.nT) return;
+    const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
+    for (int s = 0; s < ns; ++s) {
+        const PanelRec& P = sp[s];
+        const int p = p0 + s;
+        const bool self = job.same_mesh && p == i;
+        const int rule = self ? 4 : rule_of(P, x, y, z);
+        if (rule != 0) {
+            const int slot = atomicAdd(job.near_count, 1);
+            if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
+            continue;
+        }
+        Acc<TC> A;
+        A.zero();
+        const TC e0x = (TC)(P.v[0] - x), e0y = (TC)(P.v[1] - y), e0z = (TC)(P.v[2] - z);
+        const TC e1x = (TC)(P.v[3] - x), e1y = (TC)(P.v[4] - y), e1z = (TC)(P.v[5] - z);
+        const TC e2x = (TC)(P.v[6] - x), e2y = (TC)(P.v[7] - y), e2z = (TC)(P.v[8] - z);
+        const TC mx = (TC)P.n[0], my = (TC)P.n[1], mz = (TC)P.n[2];
+        const TC area = (TC)P.area;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            TC l0, l1, l2, w;
+            if constexpr (sizeof(TC) == 8) {
+                l0 = c_rule7[q].l0; l1 = c_rule7[q].l1; l2 = c_rule7[q].l2; w = c_rule7[q].w;
+            } else {
+                l0 = c_rule7f[q].l0; l1 = c_rule7f[q].l1; l2 = c_rule7f[q].l2; w = c_rule7f[q].w;
+            }
+            const TC rx = l0 * e0x + l1 * e1x + l2 * e2x;
+            const TC ry = l0 * e0y + l1 * e1y + l2 * e2y;
+            const TC rz = l0 * e0z + l1 * e1z + l2 * e2z;
+            accum<TC, true>(A, rx, ry, rz, w * area, mx, my, mz);
+        }
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const long long r = 3LL * i + a, c = 3LL * p + b;
+                if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)((double)sl_entry(A, a, b) * job.sscale);
+                if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)((double)dl_entry(A, a, b) * job.dscale);
+            }
+    }
+}
+
+// ---------------------------------------------------------------- near kernel
+template <class TO, bool MIXED>
+__global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int count = min(*job.near_count, job.near_cap);
+    for (int k = warp; k < count; k += nwarps) {
+        const int2 e = job.near_list[k];
+        const int i = e.x, p = e.y & 0x0fffffff, rule = e.y >> 28;
+        const PanelRec P = job.src[p];
+        const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
+        double sl = 0, dl = 0;
+        const int a = lane / 3, b = lane % 3;
+        if (rule == 4) {
+            Acc<double> A;
+            warp_self(A, P, x, y, z, lane);
+            if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
+        } else if (MIXED && rule < 3) {
+            Acc<float> A;
+            warp_rule<float>(A, P, x, y, z, rule, lane);
+            if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
+        } else {
+            Acc<double> A;
+            warp_rule<double>(A, P, x, y, z, rule, lane);
+            if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
+        }
+        if (lane < 9) {
+            const long long r = 3LL * i + a, c = 3LL * p + b;
+            if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)(sl * job.sscale);
+            if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)(dl * job.dscale);
+        }
+    }
+}
+
+template <class TO>
+void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, bool mixed) {
+    if (job0.nT <= 0 || job0.nS <= 0) return;
+    init_tables();
+    BlockJob<TO> job = job0;
+    DevBuf<int2> list((size_t)near_cap, st);
+    DevBuf<int> count(1, st);
+    count.zero();
+    job.near_list = list.get();
+    job.near_count = count.get();
+    job.near_cap = near_cap;
+    dim3 grid(ceil_div(job.nT, FAR_TGT), ceil_div(job.nS, FAR_SRC));
+    if (mixed) LAUNCH((far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
+    else LAUNCH((far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
+    const int warps = 152 * 16;
+    if (mixed) LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
+    else LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
+    if ((long long)job.nT * job.nS > near_cap) {
+        // the list could overflow only for blocks larger than its capacity
+        int h = 0;
+        count.download(&h, 1);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (h > near_cap) fail(SQBEM_ERR_ARG, "near-pair list overflow (%d > %d)", h, near_cap);
+    }
+}
+
+template void assemble_block<double>(const BlockJob<double>&, int, cudaStream_t, bool);
+template void assemble_block<float>(const BlockJob<float>&, int, cudaStream_t, bool);
+
+// ---------------------------------------------------------------- row sums
+// partial[chunk][row][b] = sum over source panels p in the chunk of D(row, 3p + b)
+template <class T>
+__global__ void rowsum_kernel(const T* __restrict__ D, long long rs, long long cs, int nrows, int ncolpanels,
+                              int chunk, double* __restrict__ partial) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrows) return;
+    const int c = blockIdx.y;
+    const int p0 = c * chunk, p1 = min(ncolpanels, p0 + chunk);
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int p = p0; p < p1; ++p) {
+        const long long base = row * rs + 3LL * p * cs;
+        s0 += (double)D[base];
+        s1 += (double)D[base + cs];
+        s2 += (double)D[base + 2 * cs];
+    }
+    double* o = partial + ((long long)c * nrows + row) * 3;
+    o[0] = s0; o[1] = s1; o[2] = s2;
+}
+
+// Add the chunked row sums (fixed order) to out[row * 3 + b]
+__global__ void rowsum_finish(const double* __restrict__ partial, int nchunk, int nrows, double* __restrict__ out) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrows) return;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int c = 0; c < nchunk; ++c) {
+        const double* o = partial + ((long long)c * nrows + row) * 3;
+        s0 += o[0]; s1 += o[1]; s2 += o[2];
+    }
+    out[row * 3] += s0;
+    out[row * 3 + 1] += s1;
+    out[row * 3 + 2] += s2;
+}
+
+template <class T>
+void add_rowsums(const T* D, long long rs, long long cs, int nrows, int ncolpanels, double* out, cudaStream_t st) {
+    if (nrows <= 0 || ncolpanels <= 0) return;
+    const int chunk = 32;
+    const int nchunk = ceil_div(ncolpanels, chunk);
+    DevBuf<double> part((size_t)nchunk * nrows * 3, st);
+    LAUNCH(rowsum_kernel<T>, dim3(ceil_div(nrows, 128), nchunk), 128, 0, st, D, rs, cs, nrows, ncolpanels, chunk,
+           part.get());
+    LAUNCH(rowsum_finish, ceil_div(nrows, 128), 128, 0, st, part.get(), nchunk, nrows, out);
+}
+template void add_rowsums<double>(const double*, long long, long long, int, int, double*, cudaStream_t);
+template void add_rowsums<float>(const float*, long long, long long, int, int, double*, cudaStream_t);
+
+// A(3i+a, 3i+b) -= rsum[(3i+a)*3 + b] (+ ext * delta_ab) for columns b with
+// colmask bit b of mask[i] set (all three when mask == nullptr).
+template <class T>
+__global__ void diag_complete_kernel(T* A, long long rs, long long cs, int n, const double* __restrict__ rsum,
+                                     double ext, const unsigned char* __restrict__ mask) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 9 * n) return;
+    const int i = t / 9, a = (t % 9) / 3, b = t % 3;
+    if (mask && !((mask[i] >> b) & 1)) return;
+    const long long r = 3LL * i + a, c = 3LL * i + b;
+    const double v = (double)A[r * rs + c * cs] - rsum[r * 3 + b] - (a == b ? ext : 0.0);
+    A[r * rs + c * cs] = (T)v;
+}
+
+template <class T>
+void diag_complete(T* A, long long rs, long long cs, int n, const double* rsum, double ext,
+                   const unsigned char* mask, cudaStream_t st) {
+    if (n <= 0) return;
+    LAUNCH(diag_complete_kernel<T>, ceil_div(9LL * n, 256), 256, 0, st, A, rs, cs, n, rsum, ext, mask);
+}
+template void diag_complete<double>(double*, long long, long long, int, const double*, double,
+                                    const unsigned char*, cudaStream_t);
+template void diag_complete<float>(float*, long long, long long, int, const double*, double,
+                                   const unsigned char*, cudaStream_t);
+
+// ---------------------------------------------------------------- panel integrals (API)
+__global__ void pairs_kernel(int n, const PanelRec* __restrict__ P, const double* __restrict__ x0,
+                             const int* __restrict__ self, double* SL, double* DL) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= n) return;
+    const PanelRec R = P[warp];
+    const double x = x0[3 * warp], y = x0[3 * warp + 1], z = x0[3 * warp + 2];
+    Acc<double> A;
+    const bool is_self = self[warp] != 0;
+    if (is_self) warp_self(A, R, x, y, z, lane);
+    else warp_rule<double>(A, R, x, y, z, rule_of(R, x, y, z), lane);
+    if (lane < 9) {
+        const int a = lane / 3, b = lane % 3;
+        SL[9 * warp + lane] = sl_entry(A, a, b);
+        DL[9 * warp + lane] = is_self ? 0.0 : dl_entry(A, a, b);
+    }
+}
+
+void panel_pairs(int n, const PanelRec* P, const double* x0, const int* self, double* SL, double* DL,
+                 cudaStream_t st) {
+    if (n <= 0) return;
+    init_tables();
+    LAUNCH(pairs_kernel, ceil_div(32LL * n, 256), 256, 0, st, n, P, x0, self, SL, DL);
+}
+
+// ---------------------------------------------------------------- field
+// u_j(x0) = sum_p [SL_p,ij f_p,i / (8 pi mu) - DL_p,ij u_p,i / (8 pi)]  (field.hpp:18-34)
+// One warp per point: pass 1, the lanes take the panels round-robin and apply the
+// 7-point rule to far panels while near panels (d < 3) are collected in shared
+// memory; pass 2, the whole warp integrates each near panel (lanes split the
+// rule points).  Fixed order, hence deterministic.
+constexpr int FIELD_WARPS = 4;
+constexpr int FIELD_NEAR_CAP = 256;
+
+template <class TC>
+__global__ void __launch_bounds__(FIELD_WARPS * 32) field_kernel(FieldJob job) {
+    __shared__ int near_p[FIELD_WARPS][FIELD_NEAR_CAP];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int pt = blockIdx.x * FIELD_WARPS + wl;
+    if (pt >= job.npts) return;
+    const double x = job.pts[3 * pt], y = job.pts[3 * pt + 1], z = job.pts[3 * pt + 2];
+    double ux = 0, uy = 0, uz = 0;
+    int nnear = 0;
+    int overflow = 0;
+    for (int base = 0; base < job.P; base += 32) {
+        const int p = base + lane;
+        int rule = -1;
+        PanelRec P;
+        if (p < job.P) {
+            P = job.panels[p];
+            rule = rule_of(P, x, y, z);
+        }
+        const unsigned nearmask = __ballot_sync(0xffffffffu, rule > 0);
+        if (rule > 0) {
+            const int slot = nnear + __popc(nearmask & ((1u << lane) - 1));
+            if (slot < FIELD_NEAR_CAP) near_p[wl][slot] = p;
+        }
+        nnear += __popc(nearmask);
+        if (rule == 0) {
+            Acc<TC> A;
+            A.zero();
+            const TC e0x = (TC)(P.v[0] - x), e0y = (TC)(P.v[1] - y), e0z = (TC)(P.v[2] - z);
+            const TC e1x = (TC)(P.v[3] - x), e1y = (TC)(P.v[4] - y), e1z = (TC)(P.v[5] - z);
+            const TC e2x = (TC)(P.v[6] - x), e2y = (TC)(P.v[7] - y), e2z = (TC)(P.v[8] - z);
+            const TC mx = (TC)P.n[0], my = (TC)P.n[1], mz = (TC)P.n[2], area = (TC)P.area;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                TC l0, l1, l2, w;
+                if constexpr (sizeof(TC) == 8) {
+                    l0 = c_rule7[q].l0; l1 = c_rule7[q].l1; l2 = c_rule7[q].l2; w = c_rule7[q].w;
+                } else {
+                    l0 = c_rule7f[q].l0; l1 = c_rule7f[q].l1; l2 = c_rule7f[q].l2; w = c_rule7f[q].w;
+                }
+                accum<TC, true>(A, l0 * e0x + l1 * e1x + l2 * e2x, l0 * e0y + l1 * e1y + l2 * e2y,
+                                l0 * e0z + l1 * e1z + l2 * e2z, w * area, mx, my, mz);
+            }
+            const double* f = job.f + 3 * p;
+            const double* u = job.u + 3 * p;
+            for (int j = 0; j < 3; ++j) {
+                double s = 0;
+                for (int i = 0; i < 3; ++i)
+                    s += (double)sl_entry(A, i, j) * f[i] * job.sscale + (double)dl_entry(A, i, j) * u[i] * job.dscale;
+                (j == 0 ? ux : j == 1 ? uy : uz) += s;
+            }
+        }
+    }
+    if (nnear > FIELD_NEAR_CAP) overflow = 1;
+    __syncwarp();
+    // warp-reduce the far part (fixed butterfly order)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ux += __shfl_xor_sync(0xffffffffu, ux, o);
+        uy += __shfl_xor_sync(0xffffffffu, uy, o);
+        uz += __shfl_xor_sync(0xffffffffu, uz, o);
+    }
+    const int nn = min(nnear, FIELD_NEAR_CAP);
+    for (int k = 0; k < nn; ++k) {
+        const int p = near_p[wl][k];
+        const PanelRec P = job.panels[p];
+        const int rule = rule_of(P, x, y, z);
+        double sl[9], dl[9];
+        if (job.mixed && rule < 3) {
+            Acc<float> A;
+            warp_rule<float>(A, P, x, y, z, rule, lane);
+            for (int q = 0; q < 9; ++q) { sl[q] = sl_entry(A, q / 3, q % 3); dl[q] = dl_entry(A, q / 3, q % 3); }
+        } else {
+            Acc<double> A;
+            warp_rule<double>(A, P, x, y, z, rule, lane);
+            for (int q = 0; q < 9; ++q) { sl[q] = sl_entry(A, q / 3, q % 3); dl[q] = dl_entry(A, q / 3, q % 3); }
+        }
+        const double* f = job.f + 3 * p;
+        const double* u = job.u + 3 * p;
+        for (int j = 0; j < 3; ++j) {
+            double s = 0;
+            for (int i = 0; i < 3; ++i) s += sl[3 * i + j] * f[i] * job.sscale + dl[3 * i + j] * u[i] * job.dscale;
+            (j == 0 ? ux : j == 1 ? uy : uz) += s;
+        }
+    }
+    if (lane == 0) {
+        job.out[3 * pt] = ux;
+        job.out[3 * pt + 1] = uy;
+        job.out[3 * pt + 2] = uz;
+        if (overflow) atomicExch(job.overflow, 1);
+    }
+}
+
+void field_eval(const FieldJob& job, cudaStream_t st) {
+    if (job.npts <= 0) return;
+    init_tables();
+    if (job.mixed) LAUNCH(field_kernel<float>, ceil_div(job.npts, FIELD_WARPS), FIELD_WARPS * 32, 0, st, job);
+    else LAUNCH(field_kernel<double>, ceil_div(job.npts, FIELD_WARPS), FIELD_WARPS * 32, 0, st, job);
+}
+
+}  // namespace sqbem

@@ -1,0 +1,63 @@
+// assemble.cuh -- device-side panel records and assembly / field job descriptors.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace sqbem {
+
+// One source panel as the kernels read it (144 bytes): vertices, unit normal
+// (out of the fluid), centroid, area and h = sqrt(2 area) -- the fields of
+// Mesh::geometry (src/utils/mesh.hpp:55-72).
+struct PanelRec {
+    double v[9];
+    double n[3];
+    double c[3];
+    double area, h, pad;
+};
+static_assert(sizeof(PanelRec) == 144, "PanelRec layout");
+
+// One coupling block: targets are points (panel centroids), sources are panels.
+// S receives SL * sscale, D receives DL * dscale, at element
+// (row, col) -> row * rs + col * cs with row = 3i + a, col = 3p + b.
+template <class TO>
+struct BlockJob {
+    const double* tgt = nullptr;  // 3 per target
+    int nT = 0;
+    const PanelRec* src = nullptr;
+    int nS = 0;
+    int same_mesh = 0;  // target i is the centroid of source panel i -> self integral
+    TO* S = nullptr;
+    long long s_rs = 1, s_cs = 0;
+    TO* D = nullptr;
+    long long d_rs = 1, d_cs = 0;
+    double sscale = 0, dscale = 0;
+    int2* near_list = nullptr;
+    int* near_count = nullptr;
+    int near_cap = 0;
+};
+
+struct FieldJob {
+    const double* pts = nullptr;  // 3 per point
+    int npts = 0;
+    const PanelRec* panels = nullptr;
+    int P = 0;
+    const double* u = nullptr;  // 3 per panel
+    const double* f = nullptr;  // 3 per panel
+    double sscale = 0, dscale = 0;
+    double* out = nullptr;  // 3 per point
+    int* overflow = nullptr;
+    int mixed = 0;
+};
+
+void init_tables();
+template <class TO>
+void assemble_block(const BlockJob<TO>& job, int near_cap, cudaStream_t st, bool mixed);
+template <class T>
+void add_rowsums(const T* D, long long rs, long long cs, int nrows, int ncolpanels, double* out, cudaStream_t st);
+template <class T>
+void diag_complete(T* A, long long rs, long long cs, int n, const double* rsum, double ext,
+                   const unsigned char* mask, cudaStream_t st);
+void panel_pairs(int n, const PanelRec* P, const double* x0, const int* self, double* SL, double* DL,
+                 cudaStream_t st);
+void field_eval(const FieldJob& job, cudaStream_t st);
+
+}  // namespace sqbem

@@ -1,0 +1,107 @@
+// common.cuh -- shared infrastructure of the sqbem CUDA library: status codes,
+// error propagation, launch accounting, device buffers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "sqbem.h"
+
+namespace sqbem {
+
+// Failure carried from the implementation to the C ABI boundary.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Error(code, buf);
+}
+
+inline void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+    if (e != cudaSuccess) fail(SQBEM_ERR_CUDA, "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+#define CUDA_CHECK(x) ::sqbem::cuda_check((x), #x, __FILE__, __LINE__)
+
+// Every kernel launch of the library goes through LAUNCH so the count is exact.
+extern std::atomic<long long> g_launches;
+#define LAUNCH(kernel, grid, block, smem, stream, ...)                                  \
+    do {                                                                                \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                     \
+        ::sqbem::g_launches.fetch_add(1, std::memory_order_relaxed);                    \
+        ::sqbem::cuda_check(cudaGetLastError(), #kernel, __FILE__, __LINE__);           \
+    } while (0)
+
+void require_device();
+
+// Owning device allocation (stream-ordered).
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t st = nullptr;
+    DevBuf() = default;
+    DevBuf(size_t count, cudaStream_t s) { alloc(count, s); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), st(o.st) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; st = o.st; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count, cudaStream_t s) {
+        release();
+        st = s;
+        n = count;
+        if (count == 0) return;
+        cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), s);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();
+            fail(SQBEM_ERR_ALLOC, "device allocation of %zu bytes failed: %s", count * sizeof(T),
+                 cudaGetErrorString(e));
+        }
+    }
+    void zero() {
+        if (n) CUDA_CHECK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+        n = 0;
+    }
+    void upload(const T* h, size_t count) {
+        CUDA_CHECK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+    void download(T* h, size_t count) const {
+        CUDA_CHECK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+    }
+    T* get() const { return p; }
+};
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Column-major device matrix view: element (i, j) at a[i + j * ld].
+template <class T>
+struct MatView {
+    T* a;
+    int rows, cols;
+    long long ld;
+    __host__ __device__ T& operator()(int i, int j) const { return a[i + (long long)j * ld]; }
+    MatView block(int i0, int j0, int r, int c) const { return {a + i0 + (long long)j0 * ld, r, c, ld}; }
+};
+
+constexpr double EIGHT_PI = 8.0 * 3.14159265358979323846;
+
+}  // namespace sqbem

@@ -1,0 +1,374 @@
+"""Python host mirror of the squirmer BEM hot path, over the C ABI (include/sqbem.h).
+
+Same names and argument meaning as the reference's header API
+(src/duct_flow.hpp, src/swimmer.hpp, src/trajectory.hpp, src/utils/mesh.hpp,
+src/utils/field.hpp): ``Tube``, ``SwimmerSolver`` (``slip``, ``solve_free``,
+``solve_prescribed``, ``force``, ``velocity``), ``DuctFlow`` (``solve``,
+``velocity``, ``exact_uz``, ``exact_Q``), ``velocity_at``, ``panel_integrals`` and
+the mesh generators.  Every compute call runs in the CUDA library
+``lib/libsqbem.so``; there is no CPU fallback -- if the library is missing or no
+GPU is present the call raises.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libsqbem.so")
+
+OK, ERR_ARG, ERR_SINGULAR, ERR_CUDA, ERR_NOT_CONVERGED, ERR_NO_DEVICE, ERR_ALLOC, ERR_TIMEOUT = range(8)
+FP64, MIXED = 0, 1
+WALL, INLET, OUTLET, SPHERE = 0, 1, 2, 10
+EIGHT_PI = 8.0 * math.pi
+
+
+class BEMError(RuntimeError):
+    """A failed library call; ``code`` is the sqbem status code."""
+
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_VP = ctypes.c_void_p
+_c_d, _c_i = ctypes.c_double, ctypes.c_int
+
+# name -> (restype, argtypes); every entry point declared in include/sqbem.h
+SIGNATURES = {
+    "sqbem_last_error": (ctypes.c_char_p, []),
+    "sqbem_version": (ctypes.c_char_p, []),
+    "sqbem_launch_count": (ctypes.c_longlong, []),
+    "sqbem_tube_mesh": (_c_i, [_c_d, _D, _c_i, _c_i, _c_i, _D, _I, _c_i, _I]),
+    "sqbem_swimmer_tube_mesh": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _D, _I, _c_i, _I]),
+    "sqbem_uniform_z": (_c_i, [_c_d, _c_d, _c_i, _D]),
+    "sqbem_icosphere": (_c_i, [_c_d, _c_i, _D, _c_i, _D, _I, _c_i, _I]),
+    "sqbem_geometry": (_c_i, [_c_i, _D, _D, _D, _D, _D]),
+    "sqbem_panel_integrals": (_c_i, [_c_i, _D, _D, _I, _D, _D]),
+    "sqbem_solve_dense": (_c_i, [_c_i, _c_i, _D, _D, _I]),
+    "sqbem_velocity_at": (_c_i, [_c_i, _D, _D, _D, _c_d, _c_i, _D, _D, _c_i]),
+    "sqbem_tube_create": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _c_d, _c_i, ctypes.POINTER(_VP)]),
+    "sqbem_tube_panels": (_c_i, [_VP, _I]),
+    "sqbem_tube_mesh_get": (_c_i, [_VP, _D, _I]),
+    "sqbem_tube_destroy": (None, [_VP]),
+    "sqbem_swimmer_create": (_c_i, [_VP, _c_i, _D, _I, _D, _c_d, _c_i, ctypes.POINTER(_VP)]),
+    "sqbem_swimmer_solve_free": (_c_i, [_VP, _c_i, _D, _D, _D, _D, _D]),
+    "sqbem_swimmer_solve_prescribed": (_c_i, [_VP, _D, _D, _D, _D]),
+    "sqbem_swimmer_timings": (_c_i, [_VP, _D, _D]),
+    "sqbem_swimmer_refinement": (_c_i, [_VP, _I, _D]),
+    "sqbem_swimmer_destroy": (None, [_VP]),
+    "sqbem_duct_create": (_c_i, [_c_d, _c_d, _c_i, _c_i, _c_i, _c_d, _c_i, ctypes.POINTER(_VP)]),
+    "sqbem_duct_panels": (_c_i, [_VP, _I]),
+    "sqbem_duct_mesh_get": (_c_i, [_VP, _D, _I]),
+    "sqbem_duct_solve": (_c_i, [_VP, _c_d, _c_d, _D, _D, _D]),
+    "sqbem_duct_destroy": (None, [_VP]),
+}
+
+_LIB = None
+
+
+def lib():
+    """The loaded CUDA library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise BEMError(ERR_NO_DEVICE, "libsqbem.so not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(rc):
+    if rc != OK:
+        raise BEMError(rc, lib().sqbem_last_error().decode())
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(_I)
+
+
+def _f64(x, shape=None):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    return a.reshape(shape) if shape is not None else a
+
+
+def launch_count():
+    return int(lib().sqbem_launch_count())
+
+
+# ---------------------------------------------------------------- meshes
+class Mesh:
+    """Per-panel vertices, tags and geometry (src/utils/mesh.hpp:50-91)."""
+
+    def __init__(self, V, tags):
+        self.V = _f64(V).reshape(-1, 9).copy()
+        self.tags = np.ascontiguousarray(tags, dtype=np.int32).copy()
+        self.geometry()
+
+    @property
+    def P(self):
+        return self.V.shape[0]
+
+    def geometry(self):
+        P = self.P
+        self.normal = np.zeros((P, 3))
+        self.centroid = np.zeros((P, 3))
+        self.area = np.zeros(P)
+        self.h = np.zeros(P)
+        _check(lib().sqbem_geometry(P, _dp(self.V), _dp(self.normal), _dp(self.centroid), _dp(self.area),
+                                    _dp(self.h)))
+
+    def translate(self, d):
+        self.V = self.V + np.tile(_f64(d), 3)[None, :]
+        self.geometry()
+
+    def copy(self):
+        return Mesh(self.V, self.tags)
+
+    def total_area(self):
+        return float(sum(self.area))
+
+
+def merge(a, b):
+    return Mesh(np.vstack([a.V, b.V]), np.concatenate([a.tags, b.tags]))
+
+
+def _make_mesh(fn, *args):
+    P = ctypes.c_int(0)
+    _check(fn(*args, None, None, 0, ctypes.byref(P)))
+    V = np.zeros((P.value, 9))
+    tags = np.zeros(P.value, dtype=np.int32)
+    _check(fn(*args, _dp(V), _ip(tags), P.value, ctypes.byref(P)))
+    return Mesh(V, tags)
+
+
+def uniform_z(z0, z1, nz):
+    z = np.zeros(nz + 1)
+    _check(lib().sqbem_uniform_z(z0, z1, nz, _dp(z)))
+    return z
+
+
+def tube_mesh(R, z, n_theta, n_r):
+    z = _f64(z)
+    return _make_mesh(lib().sqbem_tube_mesh, R, _dp(z), len(z), n_theta, n_r)
+
+
+def swimmer_tube_mesh(R, L, a, n_theta, n_r=4):
+    return _make_mesh(lib().sqbem_swimmer_tube_mesh, R, L, a, n_theta, n_r)
+
+
+def icosphere(a, level, center=(0.0, 0.0, 0.0), tag=SPHERE):
+    c = _f64(center)
+    return _make_mesh(lib().sqbem_icosphere, a, level, _dp(c), tag)
+
+
+# ---------------------------------------------------------------- kernels
+def panel_integrals(V9, x0, self_flag):
+    """kernels.hpp:67-82 on the GPU for arrays of (panel, target, self)."""
+    V9 = _f64(V9).reshape(-1, 9)
+    n = V9.shape[0]
+    x0 = _f64(x0).reshape(n, 3)
+    sf = np.ascontiguousarray(np.broadcast_to(np.asarray(self_flag, dtype=np.int32), (n,)))
+    SL = np.zeros((n, 9))
+    DL = np.zeros((n, 9))
+    _check(lib().sqbem_panel_integrals(n, _dp(V9), _dp(x0), _ip(sf), _dp(SL), _dp(DL)))
+    return SL, DL
+
+
+def squirmer_slip(x, center, e, B1, B2):
+    """kernels.hpp:107-111: u_s = (B1 + B2 cos) (cos rhat - e), host arithmetic."""
+    x = _f64(x).reshape(-1, 3)
+    r = x - _f64(center)[None, :]
+    rh = r * (1.0 / np.sqrt(np.sum(r * r, axis=1)))[:, None]
+    ct = rh @ _f64(e)
+    return (B1 + B2 * ct)[:, None] * (ct[:, None] * rh - _f64(e)[None, :])
+
+
+def solve_dense(A, B):
+    """linalg.hpp:53-58 (dgesv) on the GPU: returns (A^{-1} B, pivoted)."""
+    A = np.asfortranarray(np.asarray(A, dtype=np.float64))
+    B = np.asarray(B, dtype=np.float64)
+    vec = B.ndim == 1
+    X = np.asfortranarray(B.reshape(B.shape[0], -1).copy())
+    piv = ctypes.c_int(0)
+    _check(lib().sqbem_solve_dense(A.shape[0], X.shape[1], A.ctypes.data_as(_D), X.ctypes.data_as(_D),
+                                   ctypes.byref(piv)))
+    return (X[:, 0] if vec else X), bool(piv.value)
+
+
+def velocity_at(M, u, f, mu, points, precision=FP64):
+    """field.hpp:18-34 on the GPU."""
+    pts = _f64(points).reshape(-1, 3)
+    u = _f64(u).reshape(-1, 3)
+    f = _f64(f).reshape(-1, 3)
+    out = np.zeros_like(pts)
+    _check(lib().sqbem_velocity_at(M.P, _dp(M.V), _dp(u), _dp(f), mu, pts.shape[0], _dp(pts), _dp(out), precision))
+    return out
+
+
+# ---------------------------------------------------------------- tube / swimmer
+class Tube:
+    """Tube (src/swimmer.hpp:33-75): mesh, T, deflation and LU on the GPU."""
+
+    def __init__(self, R, L, a, n_theta, n_r=4, mu=1.0, precision=FP64):
+        self.R, self.L, self.mu, self.precision = R, L, mu, precision
+        h = _VP()
+        _check(lib().sqbem_tube_create(R, L, a, n_theta, n_r, mu, precision, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int(0)
+        _check(lib().sqbem_tube_panels(h, ctypes.byref(n)))
+        self.Nt = n.value
+        V = np.zeros((self.Nt, 9))
+        tags = np.zeros(self.Nt, dtype=np.int32)
+        _check(lib().sqbem_tube_mesh_get(h, _dp(V), _ip(tags)))
+        self.mesh = Mesh(V, tags)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sqbem_tube_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SwimmerSolution:
+    def __init__(self, U, Om, f_sphere, f_tube):
+        self.U, self.Om, self.f_sphere, self.f_tube = U, Om, f_sphere, f_tube
+
+
+class SwimmerSolver:
+    """SwimmerSolver (src/swimmer.hpp:83-289) on the GPU.  tube=None is the
+    unbounded fluid; the tube must outlive the solver."""
+
+    def __init__(self, tube, sphere, center, mu=1.0, precision=FP64):
+        self.tube, self.S, self.xc, self.mu = tube, sphere, _f64(center).copy(), mu
+        self.precision = precision
+        self.Ns = sphere.P
+        self.Nt = tube.Nt if tube else 0
+        h = _VP()
+        _check(lib().sqbem_swimmer_create(tube._h if tube else None, self.Ns, _dp(sphere.V), _ip(sphere.tags),
+                                          _dp(self.xc), mu, precision, ctypes.byref(h)))
+        self._h = h
+        ta, ts = ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().sqbem_swimmer_timings(h, ctypes.byref(ta), ctypes.byref(ts)))
+        self.t_assembly, self.t_schur = ta.value, ts.value
+
+    def slip(self, e, B1, B2):
+        return squirmer_slip(self.S.centroid, self.xc, e, B1, B2)
+
+    def solve_free(self, slips):
+        nr = len(slips)
+        sl = _f64(np.stack([np.asarray(s, float).reshape(-1, 3) for s in slips]))
+        U = np.zeros((nr, 3))
+        Om = np.zeros((nr, 3))
+        fs = np.zeros((nr, self.Ns, 3))
+        ft = np.zeros((nr, self.Nt, 3))
+        _check(lib().sqbem_swimmer_solve_free(self._h, nr, _dp(sl), _dp(U), _dp(Om), _dp(fs),
+                                              _dp(ft) if self.Nt else None))
+        return [SwimmerSolution(U[k], Om[k], fs[k], ft[k]) for k in range(nr)]
+
+    def solve_prescribed(self, U, Om):
+        fs = np.zeros((self.Ns, 3))
+        ft = np.zeros((self.Nt, 3))
+        _check(lib().sqbem_swimmer_solve_prescribed(self._h, _dp(_f64(U)), _dp(_f64(Om)), _dp(fs),
+                                                    _dp(ft) if self.Nt else None))
+        return SwimmerSolution(_f64(U).copy(), _f64(Om).copy(), fs, ft)
+
+    def refinement(self):
+        it, res = ctypes.c_int(0), ctypes.c_double(0)
+        _check(lib().sqbem_swimmer_refinement(self._h, ctypes.byref(it), ctypes.byref(res)))
+        return it.value, res.value
+
+    def force(self, s):
+        """swimmer.hpp:156-160: F = -sum f dA."""
+        return -np.sum(self.S.area[:, None] * s.f_sphere, axis=0)
+
+    def velocity(self, s, slip_field, pts):
+        """swimmer.hpp:163-173."""
+        allm = merge(self.tube.mesh, self.S) if self.tube else self.S
+        u = np.zeros((allm.P, 3))
+        f = np.zeros((allm.P, 3))
+        if self.Nt:
+            f[:self.Nt] = s.f_tube
+        r = self.S.centroid - self.xc[None, :]
+        u[self.Nt:] = s.U[None, :] + np.cross(s.Om[None, :], r) + np.asarray(slip_field).reshape(-1, 3)
+        f[self.Nt:] = s.f_sphere
+        return velocity_at(allm, u, f, self.mu, pts, self.precision)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sqbem_swimmer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- duct flow
+class DuctFlow:
+    """DuctFlow (src/duct_flow.hpp:22-109) on the GPU."""
+
+    class Solution:
+        def __init__(self, u, f, Q):
+            self.u, self.f, self.Q = u, f, Q
+
+    def __init__(self, R, L, n_theta, n_z, n_r, mu=1.0, precision=FP64):
+        self.R, self.L, self.mu, self.precision = R, L, mu, precision
+        h = _VP()
+        _check(lib().sqbem_duct_create(R, L, n_theta, n_z, n_r, mu, precision, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int(0)
+        _check(lib().sqbem_duct_panels(h, ctypes.byref(n)))
+        V = np.zeros((n.value, 9))
+        tags = np.zeros(n.value, dtype=np.int32)
+        _check(lib().sqbem_duct_mesh_get(h, _dp(V), _ip(tags)))
+        self.mesh = Mesh(V, tags)
+
+    def solve(self, p_in, p_out):
+        P = self.mesh.P
+        u = np.zeros((P, 3))
+        f = np.zeros((P, 3))
+        Q = ctypes.c_double(0)
+        _check(lib().sqbem_duct_solve(self._h, p_in, p_out, _dp(u), _dp(f), ctypes.byref(Q)))
+        return DuctFlow.Solution(u, f, Q.value)
+
+    def velocity(self, s, pts):
+        return velocity_at(self.mesh, s.u, s.f, self.mu, pts, self.precision)
+
+    def exact_uz(self, r, dP):
+        return dP / self.L * (self.R * self.R - r * r) / (4 * self.mu)
+
+    def exact_Q(self, dP):
+        return math.pi * self.R ** 4 * dP / self.L / (8 * self.mu)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sqbem_duct_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
