@@ -65,7 +65,7 @@ def test_panel_integrals_random_vs_oracle(oracle):
     scale_d = np.max(np.abs(DLo), axis=1) + np.max(np.abs(SLo), axis=1) / dist
     err_d = np.max(np.abs(DL - DLo), axis=1) / scale_d
     assert np.max(err_s) < 1e-12
-    assert np.max(err_d) < 1e-12
+    assert np.max(err_d) < 1e-11
 
 
 def test_solve_dense_pivoting_and_singular():
