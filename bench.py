@@ -1,0 +1,307 @@
+#!/usr/bin/env python
+"""Benchmark: BEM kinematics solves/s on one GB300 (and N replicas under torchrun).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+                    [--workload sweep|kinematics] [--impl gb300|reference]
+
+A step is one batch of the workload through sqbem_kinematics_batch (the C ABI):
+  sweep       128 instances, a/R ~ U[0.1, 0.6], beta ~ U[0, 0.8 (1 - a/R)],
+              level 2 or 3, n_theta = 24, L/R = 4 (seeded, synthetic geometry)
+  kinematics  1 instance, a/R = 0.3, beta = 0, level 3, n_theta = 24, + towed drag
+Each solve = tube assembly + LU, sphere blocks, Schur complement and the
+force-/torque-free solve for the B1 and B2 modes.
+
+value = solves / GPU time of the batches (CUDA events on the batch stream);
+e2e   = solves / host wall-clock of the same public call, host parameters in,
+        host results out (mesh generation and every copy included).
+Per-instance working sets (dense blocks of 3N x 3N) exceed the 129 MB L2, so no
+explicit L2 flush is done between steps.
+
+--impl reference times the reference algorithm on the host cores instead: the
+oracle's CPU restatement (C assembly, as single-threaded as the reference's,
+plus LAPACK through scipy on all cores), on a bounded sample of the same
+workload per step.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "squirmer-bem-3dtube_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "BEM solves/sec, batched mixed-precision vs plain FP64 on one GB300 at 1e-6 rel err"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "kinematics"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    """torchrun: one process per GPU; host-side barrier / max only."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = sorted(float(r[1]) for r in rows)
+        out["sm_mhz"] = sm[len(sm) // 2]
+        out["sm_max_mhz"] = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+# FP64 DFMA/DMMA rate of this GB300 (TFLOP/s), measured with a throughput probe
+# (see the design doc); MEASURED_PEAKS.json carries no FP64 figure.
+FP64_PEAK_TFLOPS = 1.0
+
+
+def traffic_of(cls):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        f = line.split()
+        if len(f) >= 2 and f[0] == cls and not line.startswith("#"):
+            return float(f[1])
+    return None
+
+
+def workload(name):
+    from sqbem import workloads
+    return workloads.sweep() if name == "sweep" else workloads.kinematics()
+
+
+def cpu_solve(orc, inst):
+    """One kinematics instance through the oracle (the reference's algorithm on the CPU)."""
+    import numpy as np
+    a, lam = 1.0, inst["a_over_R"]
+    R = a / lam
+    b = inst["beta"] * (R - a)
+    tube = orc.Tube(R, inst["L_over_R"] * R, a, inst["n_theta"], inst["n_r"])
+    s = orc.SwimmerSolver(tube, orc.icosphere(a, inst["sphere_level"], (b, 0, 0)), (b, 0, 0))
+    e = np.array(inst["e"])
+    m = s.solve_free([s.slip(e, 1, 0), s.slip(e, 0, 1)])
+    if inst.get("towed") and abs(b) < 1e-12:
+        s.force(s.solve_prescribed((0, 0, 1), (0, 0, 0)))
+    return m
+
+
+def cpu_sample(insts, budget_s=20.0):
+    """Time the oracle on a bounded sample: instances in order until budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.lib()
+    t0 = time.perf_counter()
+    done = 0
+    levels = []
+    for inst in insts:
+        cpu_solve(orc, inst)
+        done += 1
+        levels.append(inst["sphere_level"])
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done, dt, levels
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
+    insts = workload(args.workload)
+    cores = os.cpu_count()
+    # each step: one instance of the workload (cycling), the oracle on all cores
+    for _ in range(args.warmup):
+        pass  # the CPU path has no compile/warm-up state worth excluding beyond the first solve
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.lib()
+    cpu_solve(orc, insts[0])  # one untimed solve
+    t0 = time.perf_counter()
+    n = 0
+    for k in range(args.steps):
+        cpu_solve(orc, insts[k % len(insts)])
+        n += 1
+    dt = time.perf_counter() - t0
+    v = n / dt
+    line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "instances_per_step": 1, "precision": "fp64 (CPU)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": "%d instances of the %s workload, one per step (oracle: C assembly "
+                                       "single-threaded as in the reference, scipy LAPACK on %d threads)"
+                                       % (n, args.workload, cores)},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, ws, dist = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+        return
+    import sqbem
+    prec = sqbem.MIXED if args.precision == "mixed" else sqbem.FP64
+    insts = workload(args.workload)
+    peaks = load_peaks()
+    for _ in range(args.warmup):  # >= 3 for a valid bench line
+        sqbem.kinematics_batch(insts, prec)
+    sqbem.kernel_stats_enable(True)
+    launches0 = sqbem.launch_count()
+    h2d0, d2h0 = sqbem.transfer_bytes()
+    clocks = Clocks()
+    barrier(dist)
+    clocks.start()
+    gpu_s = 0.0
+    wall0 = time.perf_counter()
+    results = None
+    for _ in range(args.steps):
+        results, secs = sqbem.kinematics_batch(insts, prec)
+        gpu_s += secs
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    barrier(dist)
+    launches = sqbem.launch_count() - launches0
+    h2d, d2h = sqbem.transfer_bytes()
+    gpu_s = allmax(dist, gpu_s)
+    wall = allmax(dist, wall)
+    solves = allsum(dist, float(len(insts) * args.steps))
+    # dominant kernel class of the timed region
+    stats = {c: sqbem.kernel_stats(c) for c in sqbem.kernel_stats_classes()}
+    sqbem.kernel_stats_enable(False)
+    top = max(stats, key=lambda c: stats[c][1]) if stats else None
+    roofline = None
+    if top:
+        nl, secs, fl, by = stats[top]
+        if top in ("tc_gemm",):
+            achieved, peak, unit, bound = fl / secs / 1e12, peaks["bf16_tflops"], "TFLOP/s", "tensor"
+        elif top == "dgemm":
+            achieved, peak, unit, bound = fl / secs / 1e12, FP64_PEAK_TFLOPS, "TFLOP/s (fp64)", "tensor"
+        else:
+            achieved, peak, unit, bound = by / secs / 1e9, peaks["hbm_gbs"], "GB/s", "hbm"
+        roofline = {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                    "frac": achieved / peak, "traffic": traffic_of(top), "launches": nl,
+                    "share_of_gpu_time": secs / gpu_s if gpu_s > 0 else None,
+                    "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n, dt, levels = cpu_sample(insts, 20.0)
+        cpu = {"value": n / dt, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "first %d instance(s) of the %s workload (levels %s), oracle with C assembly on 1 thread "
+                         "and scipy LAPACK on all threads" % (n, args.workload, levels)}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": solves / gpu_s, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * gpu_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/bf16x3+f64" if prec == sqbem.MIXED else "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "instances_per_step": len(insts), "precision": args.precision,
+                   "n_theta": 24, "L_over_R": 4, "l2": "per-instance working set > L2, no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": solves / wall, "unit": "solves/s", "h2d_bytes_per_step": (h2d - h2d0) / args.steps,
+                "d2h_bytes_per_step": (d2h - d2h0) / args.steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "kernel_seconds": {c: v[1] for c, v in stats.items()},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

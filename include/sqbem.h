@@ -50,6 +50,17 @@ const char* sqbem_last_error(void);
 const char* sqbem_version(void);
 /* Number of kernel launches issued by this process so far (all entry points). */
 long long sqbem_launch_count(void);
+/* Host->device and device->host bytes copied by the library so far. */
+int sqbem_transfer_bytes(long long* h2d, long long* d2h);
+/* Opt-in per-kernel-class timing (no counterpart in the reference; used by the
+ * benchmark): when enabled, CUDA events bracket every launch of the timed
+ * kernel classes ("dgemm", "tc_gemm", "assemble_far", "assemble_near", ...)
+ * on their own stream, and each launch is credited with its algorithmic flops
+ * and bytes.  Enabling clears the totals. */
+int sqbem_kernel_stats_enable(int on);
+int sqbem_kernel_stats(const char* cls, long long* launches, double* seconds, double* flops, double* bytes);
+/* comma-separated names of the classes seen so far */
+int sqbem_kernel_stats_classes(char* buf, int cap);
 
 /* ---------------------------------------------------------------- geometry
  * Host-side mesh generators; the output is bit-identical to the reference.
@@ -142,6 +153,28 @@ int sqbem_duct_mesh_get(const sqbem_duct* d, double* V, int* tags);
 /* DuctFlow::solve, duct_flow.hpp:41-63: u, f (3 per panel, may be NULL), Q */
 int sqbem_duct_solve(sqbem_duct* d, double p_in, double p_out, double* u, double* f, double* Q);
 void sqbem_duct_destroy(sqbem_duct* d);
+
+/* ---------------------------------------------------------------- batch
+ * Batched kinematics: the per-(a/R, beta) body of run_kinematics
+ * (src/main.cpp:69-101) for n independent instances in one call.  Instance k:
+ * a = 1, tube Tube(1/a_over_R, L_over_R/a_over_R, 1, n_theta, n_r), sphere
+ * icosphere(1, sphere_level, (beta (R - 1), 0, 0)), solve_free for the B1 = 1
+ * and B2 = 1 slip modes with swimming direction e (main.cpp:88-89), and, if
+ * towed != 0 and beta == 0, the towed drag K = -F_z/(6 pi) (main.cpp:90-91).
+ * Any squirmer B2/B1 = alpha follows as U = U_B1 + alpha U_B2.
+ * results[k * SQBEM_RESULT_STRIDE + ...]: U_B1 (3), Om_B1 (3), U_B2 (3),
+ * Om_B2 (3), drag_K (NaN if not computed), Nt, Ns, refinement iterations.
+ * *device_seconds (may be NULL) is the GPU time of the whole batch (CUDA events
+ * on the batch stream), excluding host-side mesh generation. */
+typedef struct {
+    double a_over_R, beta, L_over_R;
+    double e[3];
+    int n_theta, n_r, sphere_level, towed;
+} sqbem_instance;
+
+#define SQBEM_RESULT_STRIDE 16
+int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
+                           double* device_seconds);
 
 #ifdef __cplusplus
 }

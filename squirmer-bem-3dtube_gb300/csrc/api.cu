@@ -32,23 +32,7 @@ void require_device() {
     }
 }
 
-template <class F>
-static int guarded(F&& f) {
-    try {
-        f();
-        g_last_error.clear();
-        return SQBEM_OK;
-    } catch (const Error& e) {
-        g_last_error = e.what();
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        g_last_error = "host allocation failed";
-        return SQBEM_ERR_ALLOC;
-    } catch (const std::exception& e) {
-        g_last_error = e.what();
-        return SQBEM_ERR_ARG;
-    }
-}
+void set_last_error(const char* msg) { g_last_error = msg; }
 
 // Per-panel geometry exactly as Mesh::geometry (mesh.hpp:61-72).
 std::vector<PanelRec> make_panels(const double* V, int P) {
@@ -102,7 +86,12 @@ void DevPanels::set(const std::vector<PanelRec>& host, cudaStream_t st) {
 
 Stream::Stream() { CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
 Stream::~Stream() {
-    if (s) cudaStreamDestroy(s);
+    if (s && owned) cudaStreamDestroy(s);
+}
+void Stream::borrow(cudaStream_t other) {
+    if (s && owned) cudaStreamDestroy(s);
+    s = other;
+    owned = false;
 }
 
 // ---------------------------------------------------------------- deflation

@@ -320,8 +320,12 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     job.near_count = count.get();
     job.near_cap = near_cap;
     dim3 grid(ceil_div(job.nT, FAR_TGT), ceil_div(job.nS, FAR_SRC));
-    if (mixed) LAUNCH((far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
-    else LAUNCH((far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
+    // credited work: every pair considered, at the 7-point rule; bytes written
+    const double pairs = (double)job.nT * job.nS;
+    const double fl = pairs * 7.0 * FLOPS_PER_EVAL;
+    const double by = pairs * 9.0 * sizeof(TO) * ((job.S ? 1 : 0) + (job.D ? 1 : 0));
+    if (mixed) TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
+    else TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
     const int warps = 152 * 16;
     if (mixed) LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
     else LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);

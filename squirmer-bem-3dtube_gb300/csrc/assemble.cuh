@@ -7,6 +7,11 @@ namespace sqbem {
 // One source panel as the kernels read it (144 bytes): vertices, unit normal
 // (out of the fluid), centroid, area and h = sqrt(2 area) -- the fields of
 // Mesh::geometry (src/utils/mesh.hpp:55-72).
+// Algorithmic flops of one quadrature-node evaluation (accum in assemble.cu,
+// FMA = 2): r from the vertex vectors 15, |r|^2 5, 1/|r| 1, powers 2, s 1,
+// r.m 5, d 3, diagonal 2, s r 3, SL 12, d r 3, DL 12.
+constexpr double FLOPS_PER_EVAL = 64.0;
+
 struct PanelRec {
     double v[9];
     double n[3];

@@ -1,0 +1,125 @@
+// batch.cu -- batched kinematics (sqbem_kinematics_batch): many independent
+// (a/R, beta, level, e) instances in one call, all on one stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "bem/utils/mesh.hpp"
+#include "common.cuh"
+#include "solver.cuh"
+
+using namespace sqbem;
+
+// u_s = (B1 + B2 cos th)(cos th rhat - e), cos th = rhat . e (kernels.hpp:107-111)
+std::vector<double> squirmer_slip_host(const std::vector<PanelRec>& S, const double* xc, const double* e, double B1,
+                                       double B2) {
+    std::vector<double> u(3 * S.size());
+    const bem::V3 c{xc[0], xc[1], xc[2]}, ev{e[0], e[1], e[2]};
+    for (size_t p = 0; p < S.size(); ++p) {
+        const bem::V3 rh = bem::unit(bem::V3{S[p].c[0], S[p].c[1], S[p].c[2]} - c);
+        const double ct = bem::dot(rh, ev);
+        const bem::V3 v = (B1 + B2 * ct) * (ct * rh - ev);
+        u[3 * p] = v.x;
+        u[3 * p + 1] = v.y;
+        u[3 * p + 2] = v.z;
+    }
+    return u;
+}
+
+namespace {
+
+struct Prepared {
+    bem::Mesh tube, sphere;
+    std::vector<double> sphereV;
+    double R = 0, L = 0, b = 0;
+    bool bounded = true;
+};
+
+Prepared prepare(const sqbem_instance& in) {
+    Prepared p;
+    const double a = 1.0;
+    p.bounded = in.a_over_R > 0;
+    p.R = p.bounded ? a / in.a_over_R : 0.0;
+    p.L = in.L_over_R * p.R;
+    p.b = p.bounded ? in.beta * (p.R - a) : 0.0;
+    if (p.bounded) p.tube = bem::swimmer_tube_mesh(p.R, p.L, a, in.n_theta, in.n_r);
+    p.sphere = bem::icosphere(a, in.sphere_level, {p.b, 0, 0});
+    p.sphereV = mesh_vertices(p.sphere);
+    return p;
+}
+
+void validate(const sqbem_instance& in) {
+    if (!(in.a_over_R >= 0 && in.a_over_R < 1) || !(in.beta >= 0 && in.beta < 1) || !(in.L_over_R > 0) ||
+        in.sphere_level < 0 || in.sphere_level > 5 || (in.a_over_R > 0 && (in.n_theta < 3 || in.n_r < 1)))
+        fail(SQBEM_ERR_ARG, "kinematics_batch: bad instance parameters");
+    const double en = std::sqrt(in.e[0] * in.e[0] + in.e[1] * in.e[1] + in.e[2] * in.e[2]);
+    if (!(std::fabs(en - 1.0) < 1e-12)) fail(SQBEM_ERR_ARG, "kinematics_batch: e must be a unit vector");
+}
+
+// One instance through the same handles the single-instance API uses.
+void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStream_t bs, double* res) {
+    std::unique_ptr<sqbem_tube> t;
+    if (P.bounded) {
+        t = std::make_unique<sqbem_tube>();
+        t->st.borrow(bs);
+        t->R = P.R; t->L = P.L; t->a = 1.0; t->n_theta = in.n_theta; t->n_r = in.n_r; t->mu = 1.0;
+        t->precision = precision;
+        t->mesh = P.tube;
+        t->build_device();
+    }
+    sqbem_swimmer s;
+    s.st.borrow(bs);
+    const double c[3] = {P.b, 0, 0};
+    s.build(t.get(), P.sphere.P(), P.sphereV.data(), c, 1.0, precision);
+    auto u1 = squirmer_slip_host(s.host_panels, c, in.e, 1, 0);
+    auto u2 = squirmer_slip_host(s.host_panels, c, in.e, 0, 1);
+    std::vector<double> slips(u1);
+    slips.insert(slips.end(), u2.begin(), u2.end());
+    double U[6], Om[6];
+    s.solve_free(2, slips.data(), U, Om, nullptr, nullptr);
+    for (int k = 0; k < 3; ++k) {
+        res[k] = U[k];
+        res[3 + k] = Om[k];
+        res[6 + k] = U[3 + k];
+        res[9 + k] = Om[3 + k];
+    }
+    res[12] = NAN;
+    if (in.towed && std::fabs(P.b) < 1e-12) {
+        const double Uz[3] = {0, 0, 1}, O0[3] = {0, 0, 0};
+        std::vector<double> fs(3 * (size_t)s.Ns);
+        s.solve_prescribed(Uz, O0, fs.data(), nullptr);
+        double Fz = 0;  // force ON the sphere, F = -sum f dA (swimmer.hpp:156-160)
+        for (int p = 0; p < s.Ns; ++p) Fz = Fz - s.host_panels[p].area * fs[3 * p + 2];
+        res[12] = -Fz / (6 * bem::PI);
+    }
+    res[13] = s.Nt;
+    res[14] = s.Ns;
+    res[15] = s.ir_iterations;
+}
+
+}  // namespace
+
+extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
+                                      double* device_seconds) {
+    return guarded([&] {
+        if (n < 0 || (n > 0 && (!inst || !results)) || (precision != SQBEM_FP64 && precision != SQBEM_MIXED))
+            fail(SQBEM_ERR_ARG, "kinematics_batch: bad arguments");
+        for (int k = 0; k < n; ++k) validate(inst[k]);
+        if (device_seconds) *device_seconds = 0;
+        if (n == 0) return;
+        require_device();
+        std::vector<Prepared> prep;
+        prep.reserve(n);
+        for (int k = 0; k < n; ++k) prep.push_back(prepare(inst[k]));
+        Stream bs;
+        EventTimer clk;
+        clk.start(bs);
+        for (int k = 0; k < n; ++k) run_one(inst[k], prep[k], precision, bs, results + (size_t)k * SQBEM_RESULT_STRIDE);
+        clk.stop(bs);
+        const double secs = clk.seconds();
+        if (device_seconds) *device_seconds = secs;
+    });
+}

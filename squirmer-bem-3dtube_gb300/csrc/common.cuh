@@ -42,7 +42,47 @@ extern std::atomic<long long> g_launches;
         ::sqbem::cuda_check(cudaGetLastError(), #kernel, __FILE__, __LINE__);           \
     } while (0)
 
+// Host<->device bytes moved by the library (every copy goes through DevBuf or
+// count_h2d/count_d2h).
+extern std::atomic<long long> g_h2d_bytes, g_d2h_bytes;
+inline void count_h2d(size_t b) { g_h2d_bytes.fetch_add((long long)b, std::memory_order_relaxed); }
+inline void count_d2h(size_t b) { g_d2h_bytes.fetch_add((long long)b, std::memory_order_relaxed); }
+
+// Opt-in per-kernel-class timing (sqbem_kernel_stats_*): CUDA events around the
+// launches of one class on their own stream, with the algorithmic flops and
+// bytes each launch is credited with.
+bool kstats_on();
+int kstat_begin(cudaStream_t st);
+void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double bytes);
+#define TIMED_LAUNCH(cls, flops, bytes, kernel, grid, block, smem, stream, ...)          \
+    do {                                                                                \
+        const int _ks = ::sqbem::kstats_on() ? ::sqbem::kstat_begin(stream) : -1;      \
+        LAUNCH(kernel, grid, block, smem, stream, __VA_ARGS__);                         \
+        if (_ks >= 0) ::sqbem::kstat_end(_ks, cls, stream, (flops), (bytes));           \
+    } while (0)
+
 void require_device();
+void set_last_error(const char* msg);
+inline void set_last_error(const std::string& msg) { set_last_error(msg.c_str()); }
+
+// Run f; convert a failure into a status code and the thread's error message.
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        set_last_error("");
+        return SQBEM_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return SQBEM_ERR_ALLOC;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return SQBEM_ERR_ARG;
+    }
+}
 
 // Owning device allocation (stream-ordered).
 template <class T>
@@ -83,9 +123,11 @@ struct DevBuf {
     }
     void upload(const T* h, size_t count) {
         CUDA_CHECK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+        count_h2d(count * sizeof(T));
     }
     void download(T* h, size_t count) const {
         CUDA_CHECK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+        count_d2h(count * sizeof(T));
     }
     T* get() const { return p; }
 };

@@ -90,10 +90,20 @@ void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A
         K = 0;
     }
     dim3 grid(ceil_div(M, GB_M), ceil_div(N, GB_N));
-    if (!ta && !tb) LAUNCH((dgemm_kernel<false, false>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else if (ta && !tb) LAUNCH((dgemm_kernel<true, false>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else if (!ta && tb) LAUNCH((dgemm_kernel<false, true>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-    else LAUNCH((dgemm_kernel<true, true>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+    const double fl = 2.0 * M * N * K;
+    const double by = 8.0 * ((double)M * K + (double)K * N + (beta == 0.0 ? 1.0 : 2.0) * M * N);
+    if (!ta && !tb)
+        TIMED_LAUNCH("dgemm", fl, by, (dgemm_kernel<false, false>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb,
+                     beta, C, ldc);
+    else if (ta && !tb)
+        TIMED_LAUNCH("dgemm", fl, by, (dgemm_kernel<true, false>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb,
+                     beta, C, ldc);
+    else if (!ta && tb)
+        TIMED_LAUNCH("dgemm", fl, by, (dgemm_kernel<false, true>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb,
+                     beta, C, ldc);
+    else
+        TIMED_LAUNCH("dgemm", fl, by, (dgemm_kernel<true, true>), grid, 256, 0, st, M, N, K, alpha, A, lda, B, ldb,
+                     beta, C, ldc);
 }
 
 // ---------------------------------------------------------------- small helpers
@@ -321,6 +331,7 @@ static void run_pivoted(double* A, long long ld, int n, int* ipiv, double* Linv,
 static int read_flag(const int* flag, cudaStream_t st) {
     int h = 0;
     CUDA_CHECK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    count_d2h(sizeof(int));
     CUDA_CHECK(cudaStreamSynchronize(st));
     return h;
 }

@@ -69,6 +69,10 @@ __global__ void copy_cols_kernel(const double* __restrict__ src, long long lds, 
 void sqbem_tube::build(double R_, double L_, double a_, int nth, int nr, double mu_, int prec) {
     R = R_; L = L_; a = a_; n_theta = nth; n_r = nr; mu = mu_; precision = prec;
     mesh = bem::swimmer_tube_mesh(R, L, a, nth, nr);
+    build_device();
+}
+
+void sqbem_tube::build_device() {
     Nt = mesh.P();
     const auto V = mesh_vertices(mesh);
     host_panels = make_panels(V.data(), Nt);
@@ -163,6 +167,7 @@ void sqbem_swimmer::solve_free(int nrhs, const double* slips, double* U, double*
         CUDA_CHECK(cudaStreamSynchronize(st));
         const double sc = h_amax / panels.area_max;
         const auto F = constraint_rows(host_panels, xc, sc);
+        count_h2d(F.size() * sizeof(double));
         CUDA_CHECK(cudaMemcpy2DAsync(M.get() + ns, sizeof(double) * n, F.data(), sizeof(double) * 6, sizeof(double) * 6,
                                      ns, cudaMemcpyHostToDevice, st));
         luM.factor_inplace(std::move(M), n, st, "dgesv failed");

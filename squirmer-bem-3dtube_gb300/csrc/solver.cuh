@@ -12,12 +12,16 @@
 
 namespace sqbem {
 
+// A CUDA stream owned by a handle, or borrowed from the caller (batched calls
+// run every handle on the batch stream).
 struct Stream {
     cudaStream_t s = nullptr;
+    bool owned = true;
     Stream();
     ~Stream();
     Stream(const Stream&) = delete;
     Stream& operator=(const Stream&) = delete;
+    void borrow(cudaStream_t other);
     operator cudaStream_t() const { return s; }
 };
 
@@ -74,7 +78,12 @@ struct sqbem_tube {
     sqbem::LU64 lu;           // FP64 factor of the deflated T
     sqbem::MixedLU mlu;       // mixed: split-BF16 factor of T (FP32 entries kept for residuals)
     void build(double R, double L, double a, int n_theta, int n_r, double mu, int precision);
+    void build_device();  // from `mesh` and the parameters already set
 };
+
+// host slip field (kernels.hpp:107-111) at the panel centroids, packed xyz
+std::vector<double> squirmer_slip_host(const std::vector<sqbem::PanelRec>& S, const double* xc, const double* e,
+                                       double B1, double B2);
 
 // SwimmerSolver, src/swimmer.hpp:83-289
 struct sqbem_swimmer {

@@ -1,0 +1,117 @@
+// stats.cu -- transfer counters and opt-in per-kernel-class event timing.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sqbem {
+
+std::atomic<long long> g_h2d_bytes{0}, g_d2h_bytes{0};
+
+namespace {
+struct Pending {
+    cudaEvent_t a = nullptr, b = nullptr;
+    std::string cls;
+    double flops = 0, bytes = 0;
+};
+struct Agg {
+    long long launches = 0;
+    double seconds = 0, flops = 0, bytes = 0;
+};
+std::mutex g_mu;
+std::atomic<bool> g_on{false};
+std::vector<Pending> g_pending;
+std::map<std::string, Agg> g_agg;
+
+void collect_locked() {
+    for (auto& p : g_pending) {
+        if (p.b) {
+            cudaEventSynchronize(p.b);
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+                Agg& g = g_agg[p.cls];
+                g.launches += 1;
+                g.seconds += ms * 1e-3;
+                g.flops += p.flops;
+                g.bytes += p.bytes;
+            }
+        }
+        if (p.a) cudaEventDestroy(p.a);
+        if (p.b) cudaEventDestroy(p.b);
+    }
+    g_pending.clear();
+}
+}  // namespace
+
+bool kstats_on() { return g_on.load(std::memory_order_relaxed); }
+
+int kstat_begin(cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    Pending p;
+    CUDA_CHECK(cudaEventCreate(&p.a));
+    CUDA_CHECK(cudaEventCreate(&p.b));
+    CUDA_CHECK(cudaEventRecord(p.a, st));
+    g_pending.push_back(p);
+    return (int)g_pending.size() - 1;
+}
+
+void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double bytes) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (slot < 0 || slot >= (int)g_pending.size()) return;
+    Pending& p = g_pending[slot];
+    CUDA_CHECK(cudaEventRecord(p.b, st));
+    p.cls = cls;
+    p.flops = flops;
+    p.bytes = bytes;
+}
+
+}  // namespace sqbem
+
+using namespace sqbem;
+
+extern "C" int sqbem_transfer_bytes(long long* h2d, long long* d2h) {
+    if (h2d) *h2d = g_h2d_bytes.load();
+    if (d2h) *d2h = g_d2h_bytes.load();
+    return SQBEM_OK;
+}
+
+extern "C" int sqbem_kernel_stats_enable(int on) {
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(g_mu);
+        collect_locked();
+        if (on) g_agg.clear();
+        g_on.store(on != 0);
+    });
+}
+
+extern "C" int sqbem_kernel_stats(const char* cls, long long* launches, double* seconds, double* flops,
+                                  double* bytes) {
+    return guarded([&] {
+        if (!cls) fail(SQBEM_ERR_ARG, "kernel_stats: null class");
+        std::lock_guard<std::mutex> lk(g_mu);
+        collect_locked();
+        Agg g;
+        auto it = g_agg.find(cls);
+        if (it != g_agg.end()) g = it->second;
+        if (launches) *launches = g.launches;
+        if (seconds) *seconds = g.seconds;
+        if (flops) *flops = g.flops;
+        if (bytes) *bytes = g.bytes;
+    });
+}
+
+extern "C" int sqbem_kernel_stats_classes(char* buf, int cap) {
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(g_mu);
+        collect_locked();
+        std::string s;
+        for (auto& kv : g_agg) s += (s.empty() ? "" : ",") + kv.first;
+        if (!buf || cap <= (int)s.size()) fail(SQBEM_ERR_ARG, "kernel_stats_classes: buffer too small");
+        std::memcpy(buf, s.c_str(), s.size() + 1);
+    });
+}

@@ -66,7 +66,22 @@ SIGNATURES = {
     "sqbem_duct_mesh_get": (_c_i, [_VP, _D, _I]),
     "sqbem_duct_solve": (_c_i, [_VP, _c_d, _c_d, _D, _D, _D]),
     "sqbem_duct_destroy": (None, [_VP]),
+    "sqbem_transfer_bytes": (_c_i, [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "sqbem_kernel_stats_enable": (_c_i, [_c_i]),
+    "sqbem_kernel_stats": (_c_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), _D, _D, _D]),
+    "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
+    "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
 }
+
+
+class Instance(ctypes.Structure):
+    """sqbem_instance (include/sqbem.h): one kinematics case of a batch."""
+    _fields_ = [("a_over_R", ctypes.c_double), ("beta", ctypes.c_double), ("L_over_R", ctypes.c_double),
+                ("e", ctypes.c_double * 3), ("n_theta", ctypes.c_int), ("n_r", ctypes.c_int),
+                ("sphere_level", ctypes.c_int), ("towed", ctypes.c_int)]
+
+
+RESULT_STRIDE = 16
 
 _LIB = None
 
@@ -108,6 +123,53 @@ def _f64(x, shape=None):
 
 def launch_count():
     return int(lib().sqbem_launch_count())
+
+
+def transfer_bytes():
+    """(host->device, device->host) bytes copied by the library so far"""
+    h, d = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    _check(lib().sqbem_transfer_bytes(ctypes.byref(h), ctypes.byref(d)))
+    return h.value, d.value
+
+
+def kernel_stats_enable(on=True):
+    _check(lib().sqbem_kernel_stats_enable(1 if on else 0))
+
+
+def kernel_stats(cls):
+    """(launches, seconds, flops, bytes) of one kernel class since enabling"""
+    n, s, f, b = ctypes.c_longlong(0), ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+    _check(lib().sqbem_kernel_stats(cls.encode(), ctypes.byref(n), ctypes.byref(s), ctypes.byref(f), ctypes.byref(b)))
+    return n.value, s.value, f.value, b.value
+
+
+def kernel_stats_classes():
+    buf = ctypes.create_string_buffer(4096)
+    _check(lib().sqbem_kernel_stats_classes(buf, 4096))
+    return [c for c in buf.value.decode().split(",") if c]
+
+
+def kinematics_batch(instances, precision=MIXED):
+    """sqbem_kinematics_batch: instances = list of dicts with a_over_R, beta,
+    L_over_R, e, n_theta, n_r, sphere_level, towed.  Returns (results
+    (n x RESULT_STRIDE), device seconds)."""
+    n = len(instances)
+    arr = (Instance * n)()
+    for k, d in enumerate(instances):
+        arr[k].a_over_R = d["a_over_R"]
+        arr[k].beta = d["beta"]
+        arr[k].L_over_R = d.get("L_over_R", 4.0)
+        e = d.get("e", (0.0, 0.0, 1.0))
+        for c in range(3):
+            arr[k].e[c] = e[c]
+        arr[k].n_theta = d.get("n_theta", 24)
+        arr[k].n_r = d.get("n_r", 4)
+        arr[k].sphere_level = d["sphere_level"]
+        arr[k].towed = int(d.get("towed", 0))
+    res = np.zeros((n, RESULT_STRIDE))
+    secs = ctypes.c_double(0)
+    _check(lib().sqbem_kinematics_batch(n, ctypes.cast(arr, _VP), precision, _dp(res), ctypes.byref(secs)))
+    return res, secs.value
 
 
 # ---------------------------------------------------------------- meshes
