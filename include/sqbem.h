@@ -98,6 +98,14 @@ int sqbem_panel_integrals(int n, const double* V9, const double* x0, const int* 
  * message "dgesv failed". */
 int sqbem_solve_dense(int n, int nrhs, const double* A, double* B, int* pivoted);
 
+/* gemm, src/utils/linalg.hpp:42-48, in the form the SQBEM_MIXED path uses:
+ * C = alpha A B + beta C for column-major FP32 host arrays (A: M x K, B: K x N,
+ * C: M x N), with A and B split into BF16 hi and lo parts and the products
+ * hi*hi + hi*lo + lo*hi accumulated in FP32 on the tensor cores (tcgen05).
+ * Relative accuracy about 2^-16 per product. */
+int sqbem_gemm_mixed(int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
+                     float beta, float* C, int ldc);
+
 /* ---------------------------------------------------------------- field
  * velocity_at, src/utils/field.hpp:18-34: lab-frame velocity at npts points
  * from the boundary solution (u, f per panel) on the P panels V. */

@@ -1,0 +1,480 @@
+// tc_gemm.cu -- persistent grouped GEMM on the 5th-generation tensor cores
+// (tcgen05.mma, accumulators in tensor memory, operands staged by TMA).
+//
+// CTA = 6 warps, one CTA per SM:
+//   warp 0     TMA producer: for every k-block of 64 loads the four 128 x 64 BF16
+//              tiles (A_hi, A_lo, B_hi, B_lo; 128-byte swizzle) into a stage of a
+//              3-stage shared-memory ring, completion tracked by mbarriers.
+//   warp 1     allocates 256 TMEM columns (two 128 x 128 FP32 accumulators) and
+//              issues, from one lane, 3 x 4 tcgen05.mma (M = 128, N = 128,
+//              K = 16) per k-block: hi*hi + hi*lo + lo*hi; tcgen05.commit frees
+//              the stage and, after the last k-block, hands the accumulator to
+//              the epilogue.
+//   warps 2-5  epilogue: tcgen05.ld (32 lanes x 32 columns per instruction; warp
+//              w reads TMEM lanes 32 (w % 4) ..), alpha / beta, FP32 store and
+//              optional split-BF16 stores, then release the accumulator.
+// Two accumulators let the epilogue of tile t overlap the MMAs of tile t + 1.
+// Tiles of all problems are enumerated in one list; CTA b takes tiles b,
+// b + gridDim, ...  Every mbarrier wait is bounded (about 2 s of SM clock); on
+// expiry the kernel raises *err, drains its own copies and MMAs, frees its TMEM
+// and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "tc_gemm.cuh"
+
+namespace sqbem {
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int STAGES = 3;
+constexpr int TILE_BYTES = BM * BK * 2;            // 16 KB (A and B tiles alike)
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;        // A_hi, A_lo, B_hi, B_lo
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int TMEM_COLS = 256;
+constexpr int NTHREADS = 192;
+constexpr long long WAIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity; false (and *err = 1) on expiry
+// or if another role already gave up.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (;;) {
+        if (mbar_try(bar, parity)) return true;
+        if (*(volatile int*)err) return false;
+        if (clock64() - t0 > WAIT_CYCLES) {
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((unsigned long long)map) : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
+}
+
+// Instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 lanes x 32 consecutive FP32 columns from tensor memory.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct KArgs {
+    const TcProblem* probs;
+    const CUtensorMap* maps;  // 4 per problem: A_hi, A_lo, B_hi, B_lo
+    int nprob;
+    int total_tiles;
+    int* err;
+    int* flag;
+};
+
+__device__ __forceinline__ int find_problem(const TcProblem* probs, int nprob, int t) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {  // last problem with tile_start <= t
+        const int mid = (lo + hi + 1) >> 1;
+        if (probs[mid].tile_start <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(KArgs args) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+    const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
+    const uint32_t done_bar = smem_u32(bars + 2 * STAGES + 4);
+    uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int* err = args.err;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, 128);
+        }
+        mbar_init(done_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer
+        int s = 0;
+        uint32_t ph = 0;
+        int armed[STAGES] = {};
+        int last_p = -1;
+        for (int t = blockIdx.x; t < args.total_tiles; t += gridDim.x) {
+            const int p = find_problem(args.probs, args.nprob, t);
+            const TcProblem& P = args.probs[p];
+            const CUtensorMap* m = args.maps + 4 * p;
+            if (p != last_p) {
+                for (int j = 0; j < 4; ++j) tensormap_acquire(m + j);
+                last_p = p;
+            }
+            const int local = t - P.tile_start;
+            const int tm = local / P.tiles_n, tn = local % P.tiles_n;
+            const int nkb = (P.K + BK - 1) / BK;
+            bool ok = true;
+            for (int kb = 0; kb < nkb; ++kb) {
+                if (!mbar_wait(empty0 + 8 * s, ph ^ 1, err)) { ok = false; break; }
+                const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+                const uint32_t fb = full0 + 8 * s;
+                mbar_expect_tx(fb, STAGE_BYTES);
+                tma_load_2d(st, m + 0, kb * BK, tm * BM, fb);
+                tma_load_2d(st + TILE_BYTES, m + 1, kb * BK, tm * BM, fb);
+                tma_load_2d(st + 2 * TILE_BYTES, m + 2, kb * BK, tn * BN, fb);
+                tma_load_2d(st + 3 * TILE_BYTES, m + 3, kb * BK, tn * BN, fb);
+                armed[s] += 1;
+                if (++s == STAGES) { s = 0; ph ^= 1; }
+            }
+            if (!ok) break;
+        }
+        // drain: every armed stage must have completed before the CTA exits
+        for (int q = 0; q < STAGES; ++q)
+            if (armed[q] > 0) {
+                const uint32_t par = (uint32_t)((armed[q] - 1) & 1);
+                const long long t0 = clock64();
+                while (!mbar_try(full0 + 8 * q, par) && clock64() - t0 < WAIT_CYCLES) {
+                }
+            }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer
+        int s = 0;
+        uint32_t ph = 0;
+        int acc = 0;
+        uint32_t aph = 0;
+        for (int t = blockIdx.x; t < args.total_tiles; t += gridDim.x) {
+            const int p = find_problem(args.probs, args.nprob, t);
+            const int nkb = (args.probs[p].K + BK - 1) / BK;
+            if (!mbar_wait(tempty0 + 8 * acc, aph ^ 1, err)) break;
+            tc_fence_after();
+            const uint32_t d = tmem_base + (uint32_t)(acc * BN);
+            bool ok = true;
+            for (int kb = 0; kb < nkb; ++kb) {
+                if (!mbar_wait(full0 + 8 * s, ph, err)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+                const uint64_t ah = smem_desc(st), al = smem_desc(st + TILE_BYTES);
+                const uint64_t bh = smem_desc(st + 2 * TILE_BYTES), bl = smem_desc(st + 3 * TILE_BYTES);
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+                    const uint64_t off = (uint64_t)(k * 32) >> 4;  // 16 BF16 = 32 bytes along K
+                    mma_bf16(d, ah + off, bh + off, (kb > 0 || k > 0) ? 1u : 0u);
+                    mma_bf16(d, ah + off, bl + off, 1u);
+                    mma_bf16(d, al + off, bh + off, 1u);
+                }
+                mma_commit(empty0 + 8 * s);
+                if (++s == STAGES) { s = 0; ph ^= 1; }
+            }
+            if (!ok) break;
+            mma_commit(tfull0 + 8 * acc);
+            if (++acc == 2) { acc = 0; aph ^= 1; }
+        }
+        // all MMAs issued by this CTA complete before TMEM is released
+        mma_commit(done_bar);
+        const long long t0 = clock64();
+        while (!mbar_try(done_bar, 0) && clock64() - t0 < WAIT_CYCLES) {
+        }
+    } else if (warp >= 2) {
+        // ---------------- epilogue
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int acc = 0;
+        uint32_t aph = 0;
+        int any_big = 0;
+        for (int t = blockIdx.x; t < args.total_tiles; t += gridDim.x) {
+            const int p = find_problem(args.probs, args.nprob, t);
+            const TcProblem& P = args.probs[p];
+            const int local = t - P.tile_start;
+            const int tm = local / P.tiles_n, tn = local % P.tiles_n;
+            if (!mbar_wait(tfull0 + 8 * acc, aph, err)) break;
+            tc_fence_after();
+            const int m = tm * BM + row;
+            const bool row_ok = m < P.M;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * BN + c0), v);
+                if (!row_ok) continue;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int n = tn * BN + c0 + j;
+                    if (n >= P.N) break;
+                    float x = P.alpha * v[j];
+                    if (P.C) {
+                        float* c = P.C + (long long)m * P.c_rs + (long long)n * P.c_cs;
+                        if (P.beta != 0.f) x = fmaf(P.beta, *c, x);
+                        *c = x;
+                    }
+                    if (P.check_unit && !(fabsf(x) <= 1.f)) any_big = 1;
+                    if (P.O_hi) {
+                        const bf16 h = __float2bfloat16_rn(x);
+                        const bf16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+                        const long long o = (long long)m * P.o_rs + (long long)n * P.o_cs;
+                        P.O_hi[o] = h;
+                        P.O_lo[o] = l;
+                    }
+                    if (P.P_hi) {
+                        const bf16 h = __float2bfloat16_rn(x);
+                        const bf16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+                        const long long o = (long long)m * P.p_rs + (long long)n * P.p_cs;
+                        P.P_hi[o] = h;
+                        P.P_lo[o] = l;
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(tempty0 + 8 * acc);
+            if (++acc == 2) { acc = 0; aph ^= 1; }
+        }
+        if (any_big && args.flag) atomicOr(args.flag, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------- split conversion
+__global__ void split_kernel(const float* __restrict__ src, long long s_rs, long long s_cs, int rows, int cols,
+                             bf16* __restrict__ hi, bf16* __restrict__ lo, long long d_rs, long long d_cs) {
+    // iterate with the destination's contiguous index fastest
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)rows * cols) return;
+    int r, c;
+    if (d_rs == 1) { r = (int)(t % rows); c = (int)(t / rows); }
+    else { c = (int)(t % cols); r = (int)(t / cols); }
+    const float x = src[r * s_rs + c * s_cs];
+    const bf16 h = __float2bfloat16_rn(x);
+    hi[r * d_rs + c * d_cs] = h;
+    lo[r * d_rs + c * d_cs] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+void get_encode() {
+    std::call_once(g_encode_once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        CUDA_CHECK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) fail(SQBEM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    });
+}
+
+// Tensor map of a K-major BF16 plane: rows x k, row pitch ld elements, boxes of
+// 128 rows x 64 k with 128-byte swizzle, zero fill outside the matrix.
+CUtensorMap make_map(const bf16* base, int rows, int k, long long ld) {
+    if (((uintptr_t)base & 15) != 0 || (ld * 2) % 16 != 0 || rows <= 0 || k <= 0)
+        fail(SQBEM_ERR_ARG, "tensor map: misaligned operand (ld %lld)", ld);
+    CUtensorMap m;
+    cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+    cuuint32_t box[2] = {BK, BM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(SQBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return m;
+}
+
+int g_num_sms = 0;
+
+}  // namespace
+
+void split_convert(const float* src, long long s_rs, long long s_cs, int rows, int cols, bf16* hi, bf16* lo,
+                   long long d_rs, long long d_cs, cudaStream_t st) {
+    if (rows <= 0 || cols <= 0) return;
+    LAUNCH(split_kernel, ceil_div((long long)rows * cols, 256), 256, 0, st, src, s_rs, s_cs, rows, cols, hi, lo, d_rs,
+           d_cs);
+}
+
+void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperands>& ops, int* err, int* flag,
+             cudaStream_t st) {
+    if (probs_in.size() != ops.size()) fail(SQBEM_ERR_ARG, "tc_gemm: operand count");
+    get_encode();
+    std::vector<TcProblem> probs;
+    std::vector<CUtensorMap> maps;
+    int total = 0;
+    double flops = 0, bytes = 0;
+    for (size_t i = 0; i < probs_in.size(); ++i) {
+        TcProblem P = probs_in[i];
+        const TcOperands& o = ops[i];
+        if (P.M <= 0 || P.N <= 0) continue;
+        if (P.K <= 0) fail(SQBEM_ERR_ARG, "tc_gemm: K must be positive");
+        if (o.A.rows < P.M || o.A.k < P.K || o.B.rows < P.N || o.B.k < P.K)
+            fail(SQBEM_ERR_ARG, "tc_gemm: operand smaller than the problem");
+        P.tiles_n = ceil_div(P.N, BN);
+        P.tile_start = total;
+        total += ceil_div(P.M, BM) * P.tiles_n;
+        probs.push_back(P);
+        // maps cover exactly the problem's extent: rows beyond M / N and k beyond K read as zero
+        maps.push_back(make_map(o.A.hi, P.M, P.K, o.A.ld));
+        maps.push_back(make_map(o.A.lo, P.M, P.K, o.A.ld));
+        maps.push_back(make_map(o.B.hi, P.N, P.K, o.B.ld));
+        maps.push_back(make_map(o.B.lo, P.N, P.K, o.B.ld));
+        flops += 2.0 * P.M * P.N * P.K;
+        bytes += 4.0 * ((double)P.M * P.K + (double)P.K * P.N) + 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
+    }
+    if (total == 0) return;
+    if (!g_num_sms) {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    }
+    DevBuf<TcProblem> dprobs(probs.size(), st);
+    DevBuf<CUtensorMap> dmaps(maps.size(), st);
+    dprobs.upload(probs.data(), probs.size());
+    dmaps.upload(maps.data(), maps.size());
+    KArgs a;
+    a.probs = dprobs.get();
+    a.maps = dmaps.get();
+    a.nprob = (int)probs.size();
+    a.total_tiles = total;
+    a.err = err;
+    a.flag = flag;
+    const int grid = std::min(total, g_num_sms);
+    TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
+}
+
+}  // namespace sqbem
+
+using namespace sqbem;
+
+extern "C" int sqbem_gemm_mixed(int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
+                                float beta, float* C, int ldc) {
+    return guarded([&] {
+        if (M < 0 || N < 0 || K <= 0 || !A || !B || !C || lda < M || ldb < K || ldc < M)
+            fail(SQBEM_ERR_ARG, "gemm_mixed: bad arguments");
+        if (M == 0 || N == 0) return;
+        require_device();
+        cudaStream_t st;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        {
+            const long long ld = pad_ld(K);
+            DevBuf<float> dA((size_t)lda * K, st), dB((size_t)ldb * N, st), dC((size_t)ldc * N, st);
+            DevBuf<bf16> ah((size_t)M * ld, st), al((size_t)M * ld, st), bh((size_t)N * ld, st), bl((size_t)N * ld, st);
+            DevBuf<int> err(1, st);
+            err.zero();
+            dA.upload(A, (size_t)lda * K);
+            dB.upload(B, (size_t)ldb * N);
+            dC.upload(C, (size_t)ldc * N);
+            // A (col-major M x K) -> K-major rows; B (col-major K x N) -> K-major columns
+            split_convert(dA.get(), 1, lda, M, K, ah.get(), al.get(), ld, 1, st);
+            split_convert(dB.get(), 1, ldb, K, N, bh.get(), bl.get(), 1, ld, st);
+            TcProblem P;
+            P.M = M; P.N = N; P.K = K; P.alpha = alpha; P.beta = beta;
+            P.C = dC.get(); P.c_rs = 1; P.c_cs = ldc;
+            TcOperands o;
+            o.A = {ah.get(), al.get(), M, K, ld};
+            o.B = {bh.get(), bl.get(), N, K, ld};
+            tc_gemm({P}, {o}, err.get(), nullptr, st);
+            int h_err = 0;
+            err.download(&h_err, 1);
+            dC.download(C, (size_t)ldc * N);
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            if (h_err) fail(SQBEM_ERR_TIMEOUT, "gemm_mixed: a bounded wait in the tensor-core GEMM expired");
+        }
+        cudaStreamDestroy(st);
+    });
+}

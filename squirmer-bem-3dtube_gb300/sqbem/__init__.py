@@ -71,7 +71,24 @@ SIGNATURES = {
     "sqbem_kernel_stats": (_c_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), _D, _D, _D]),
     "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
     "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
+    "sqbem_gemm_mixed": (_c_i, [_c_i, _c_i, _c_i, ctypes.c_float, ctypes.POINTER(ctypes.c_float), _c_i,
+                                ctypes.POINTER(ctypes.c_float), _c_i, ctypes.c_float,
+                                ctypes.POINTER(ctypes.c_float), _c_i]),
 }
+
+
+def gemm_mixed(A, B, C=None, alpha=1.0, beta=0.0):
+    """linalg.hpp:42-48 gemm on the tensor cores, split-BF16 operands: returns
+    alpha A B + beta C as FP32."""
+    A = np.asfortranarray(np.asarray(A, dtype=np.float32))
+    B = np.asfortranarray(np.asarray(B, dtype=np.float32))
+    M, K = A.shape
+    N = B.shape[1]
+    Cm = np.asfortranarray(np.zeros((M, N), np.float32) if C is None else np.asarray(C, dtype=np.float32).copy())
+    fp = ctypes.POINTER(ctypes.c_float)
+    _check(lib().sqbem_gemm_mixed(M, N, K, alpha, A.ctypes.data_as(fp), M, B.ctypes.data_as(fp), K, beta,
+                                  Cm.ctypes.data_as(fp), M))
+    return Cm
 
 
 class Instance(ctypes.Structure):
