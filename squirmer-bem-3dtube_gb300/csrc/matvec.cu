@@ -1,0 +1,175 @@
+// matvec.cu -- grouped FP64-accumulated matrix-vector products and helpers.
+//
+// matvec: one thread per row, columns split into chunks of MV_CHUNK across
+// blockIdx.y (coalesced column-major reads, the vector broadcast); chunk partial
+// sums land in a scratch array and are added in chunk order by a second kernel,
+// so the result does not depend on scheduling.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "matvec.cuh"
+
+namespace sqbem {
+
+namespace {
+
+constexpr int MV_ROWS = 128;
+constexpr int MV_CHUNK = 64;
+constexpr int MV_RMAX = 8;
+
+constexpr int MAXJOBS = 48;
+struct MvDev {
+    MvJob j;
+    long long part_off;  // offset of this job's partials in the scratch
+    int nchunk;
+};
+struct MvArgs {
+    int n;
+    MvDev j[MAXJOBS];
+};
+struct CopyArgs {
+    int n;
+    CopyJob j[MAXJOBS];
+};
+struct NormArgs {
+    int n;
+    NormJob j[MAXJOBS];
+};
+
+__global__ void __launch_bounds__(MV_ROWS) mv_partial(const __grid_constant__ MvArgs args, double* __restrict__ part) {
+    const MvDev& D = args.j[blockIdx.z];
+    const MvJob& J = D.j;
+    const int row = blockIdx.x * MV_ROWS + threadIdx.x;
+    const int c = blockIdx.y;
+    if (c >= D.nchunk || row >= J.m) return;
+    const int j0 = c * MV_CHUNK, j1 = min(J.n, j0 + MV_CHUNK);
+    double s[MV_RMAX];
+#pragma unroll
+    for (int k = 0; k < MV_RMAX; ++k) s[k] = 0.0;
+    for (int j = j0; j < j1; ++j) {
+        const double a = J.A32 ? (double)J.A32[row + (long long)j * J.lda] : J.A64[row + (long long)j * J.lda];
+#pragma unroll
+        for (int k = 0; k < MV_RMAX; ++k)
+            if (k < J.r) s[k] = fma(a, J.x[j + (long long)k * J.ldx], s[k]);
+    }
+    double* o = part + D.part_off + ((long long)c * J.m + row) * MV_RMAX;
+#pragma unroll
+    for (int k = 0; k < MV_RMAX; ++k) o[k] = s[k];
+}
+
+__global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __restrict__ part) {
+    const MvDev& D = args.j[blockIdx.y];
+    const MvJob& J = D.j;
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= J.m) return;
+    for (int k = 0; k < J.r; ++k) {
+        double s = 0.0;
+        for (int c = 0; c < D.nchunk; ++c) s += part[D.part_off + ((long long)c * J.m + row) * MV_RMAX + k];
+        double* y = J.y + row + (long long)k * J.ldy;
+        *y = J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * *y);
+    }
+}
+
+__global__ void copy_kernel_g(const __grid_constant__ CopyArgs args) {
+    const CopyJob& J = args.j[blockIdx.y];
+    const long long total = (long long)J.rows * J.cols;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(t % J.rows), c = (int)(t / J.rows);
+        const double s = J.s64 ? J.s64[r + c * J.lds] : (double)J.s32[r + c * J.lds];
+        if (J.d64) {
+            double* d = J.d64 + r + c * J.ldd;
+            *d = J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * *d);
+        } else {
+            float* d = J.d32 + r + c * J.ldd;
+            *d = (float)(J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * (double)*d));
+        }
+    }
+}
+
+// one block per (job, column): fixed-order tree reduction
+__global__ void sumsq_kernel(const __grid_constant__ NormArgs args) {
+    __shared__ double red[256];
+    const NormJob& J = args.j[blockIdx.y];
+    const int c = blockIdx.x;
+    if (c >= J.cols) return;
+    double s = 0.0;
+    for (int r = threadIdx.x; r < J.rows; r += blockDim.x) {
+        const double v = J.x[r + (long long)c * J.ldx];
+        s = fma(v, v, s);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) J.out[c] = red[0];
+}
+
+}  // namespace
+
+void matvec_group(const std::vector<MvJob>& jobs_in, cudaStream_t st) {
+    std::vector<MvJob> jobs;
+    for (const MvJob& j : jobs_in)
+        if (j.m > 0 && j.r > 0) {
+            if (j.r > MV_RMAX) fail(SQBEM_ERR_ARG, "matvec: at most %d right-hand sides", MV_RMAX);
+            jobs.push_back(j);
+        }
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        MvArgs a;
+        a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        long long off = 0;
+        int maxm = 0, maxc = 0;
+        double bytes = 0;
+        for (int k = 0; k < a.n; ++k) {
+            const MvJob& j = jobs[i0 + k];
+            a.j[k].j = j;
+            a.j[k].nchunk = std::max(1, ceil_div(j.n, MV_CHUNK));
+            a.j[k].part_off = off;
+            off += (long long)a.j[k].nchunk * j.m * MV_RMAX;
+            maxm = std::max(maxm, j.m);
+            maxc = std::max(maxc, a.j[k].nchunk);
+            bytes += (double)j.m * j.n * (j.A32 ? 4 : 8);
+        }
+        DevBuf<double> part((size_t)off, st);
+        TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial, dim3(ceil_div(maxm, MV_ROWS), maxc, (unsigned)a.n), MV_ROWS, 0,
+                     st, a, part.get());
+        LAUNCH(mv_finish, dim3(ceil_div(maxm, 128), (unsigned)a.n), 128, 0, st, a, part.get());
+    }
+}
+
+void copy_group(const std::vector<CopyJob>& jobs_in, cudaStream_t st) {
+    std::vector<CopyJob> jobs;
+    for (const CopyJob& j : jobs_in)
+        if (j.rows > 0 && j.cols > 0) jobs.push_back(j);
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        CopyArgs a;
+        a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        long long mx = 0;
+        for (int k = 0; k < a.n; ++k) {
+            a.j[k] = jobs[i0 + k];
+            mx = std::max(mx, (long long)a.j[k].rows * a.j[k].cols);
+        }
+        LAUNCH(copy_kernel_g, dim3((unsigned)std::min<long long>(ceil_div(mx, 256), 2048), (unsigned)a.n), 256, 0, st,
+               a);
+    }
+}
+
+void sumsq_group(const std::vector<NormJob>& jobs, cudaStream_t st) {
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        NormArgs a;
+        a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        int mc = 0;
+        for (int k = 0; k < a.n; ++k) {
+            a.j[k] = jobs[i0 + k];
+            mc = std::max(mc, a.j[k].cols);
+        }
+        if (mc == 0) continue;
+        LAUNCH(sumsq_kernel, dim3(mc, (unsigned)a.n), 256, 0, st, a);
+    }
+}
+
+}  // namespace sqbem

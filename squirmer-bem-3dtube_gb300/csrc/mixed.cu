@@ -1,0 +1,391 @@
+// mixed.cu -- recursive LU and triangular solves on the split-BF16 tensor-core
+// GEMM, grouped over equally sized matrices (see mixed.cuh).
+//
+// LU(c0, w)   factors the panel of columns [c0, c0 + w) over rows [c0, n):
+//             w = 128: leaf -- the 128 x 128 diagonal block is factored and its
+//             triangles inverted in shared memory (diag_kernel), then
+//             L21 = A21 U11^{-1} on the tensor cores (certified |L21| <= 1);
+//             otherwise LU(left half), U12 = L11^{-1} A12 (TRSM_L), the Schur
+//             update A22 -= L21 U12 with K = w/2, and LU(right half).
+// TRSM_L/U    solve with the unit-lower / upper factor: leaf X = L^{-1}_b B or
+//             U^{-1}_b B with the stored block inverses; otherwise two halves and
+//             one GEMM update with K = w/2.
+// Operand layouts: the left operand of every GEMM is K-major along rows
+// (row-major split copy R), the right operand K-major along columns
+// (column-major split copy C); each producer step writes the copies its
+// consumers need.  FP32 master values are updated by the GEMM epilogues.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "mixed.cuh"
+#include "tc_gemm.cuh"
+
+namespace sqbem {
+
+void MixedLU::alloc(int nt, cudaStream_t st) {
+    n_true = nt;
+    n = pad128(nt);
+    const size_t nn = (size_t)n * n, nb = (size_t)(n / MX_NB) * MX_NB * MX_NB;
+    A.alloc(nn, st);
+    Rh.alloc(nn, st); Rl.alloc(nn, st);
+    Ch.alloc(nn, st); Cl.alloc(nn, st);
+    Li.alloc(nb, st); Ui.alloc(nb, st);
+    LiRh.alloc(nb, st); LiRl.alloc(nb, st);
+    UiRh.alloc(nb, st); UiRl.alloc(nb, st);
+    UiCh.alloc(nb, st); UiCl.alloc(nb, st);
+}
+
+namespace {
+
+// ---------------------------------------------------------------- conversion
+constexpr int MAXJOBS = 64;
+struct ConvArgs {
+    int n;
+    ConvJob j[MAXJOBS];
+};
+
+__global__ void conv_kernel(const __grid_constant__ ConvArgs args) {
+    const ConvJob& J = args.j[blockIdx.y];
+    const long long total = (long long)J.rows * J.cols;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int r, c;
+        if (J.d_rs == 1) { r = (int)(t % J.rows); c = (int)(t / J.rows); }
+        else { c = (int)(t % J.cols); r = (int)(t / J.cols); }
+        const float x = J.src[r * J.s_rs + c * J.s_cs];
+        const bf16 h = __float2bfloat16_rn(x);
+        J.hi[r * J.d_rs + c * J.d_cs] = h;
+        J.lo[r * J.d_rs + c * J.d_cs] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+}
+
+// ---------------------------------------------------------------- diagonal leaf
+struct DiagJob {
+    float* A;  // the 128 x 128 block, column-major, leading dimension lda
+    long long lda;
+    float* Li;
+    float* Ui;
+    bf16 *LiRh, *LiRl, *UiRh, *UiRl, *UiCh, *UiCl;
+};
+
+constexpr int DIAG_THREADS = 512;
+constexpr int DP = MX_NB + 1;  // padded row of the shared block
+
+__device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x) {
+    const bf16 a = __float2bfloat16_rn(x);
+    h[i] = a;
+    l[i] = __float2bfloat16_rn(x - __bfloat162float(a));
+}
+
+// LU of the block without exchanges, flagging |l| > 1 (bit 0) and a zero or
+// non-finite pivot (bit 1); then L^{-1} by forward and U^{-1} by backward
+// elimination applied to the identity.
+struct DiagArgs {
+    int* flag;
+    DiagJob j[MAXJOBS];
+};
+
+__global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constant__ DiagArgs args) {
+    extern __shared__ float sh[];
+    float(*a)[DP] = reinterpret_cast<float(*)[DP]>(sh);
+    float(*x)[DP] = reinterpret_cast<float(*)[DP]>(sh + MX_NB * DP);
+    const DiagJob& J = args.j[blockIdx.x];
+    int* flag = args.flag;
+    const int tid = threadIdx.x;
+    constexpr int N = MX_NB;
+    for (int e = tid; e < N * N; e += DIAG_THREADS) a[e % N][e / N] = J.A[(e % N) + (e / N) * J.lda];
+    __syncthreads();
+    int bad = 0;
+    for (int j = 0; j < N; ++j) {
+        const float piv = a[j][j];
+        if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+        for (int i = j + 1 + tid; i < N; i += DIAG_THREADS) {
+            const float l = a[i][j] / piv;
+            a[i][j] = l;
+            if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+        }
+        __syncthreads();
+        const int w = N - 1 - j;
+        for (int e = tid; e < w * w; e += DIAG_THREADS) {
+            const int i = j + 1 + e % w, c = j + 1 + e / w;
+            a[i][c] = fmaf(-a[i][j], a[j][c], a[i][c]);
+        }
+        __syncthreads();
+    }
+    if (bad) atomicOr(flag, bad);
+    for (int e = tid; e < N * N; e += DIAG_THREADS) J.A[(e % N) + (e / N) * J.lda] = a[e % N][e / N];
+    // L^{-1}
+    for (int e = tid; e < N * N; e += DIAG_THREADS) x[e / N][e % N] = (e / N == e % N) ? 1.f : 0.f;
+    __syncthreads();
+    for (int j = 0; j < N - 1; ++j) {
+        const int w = N - 1 - j;
+        for (int e = tid; e < w * (j + 1); e += DIAG_THREADS) {
+            const int i = j + 1 + e % w, c = e / w;
+            x[i][c] = fmaf(-a[i][j], x[j][c], x[i][c]);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e % N, c = e / N;
+        J.Li[r + c * N] = x[r][c];
+        put_split(J.LiRh, J.LiRl, (long long)r * N + c, x[r][c]);
+    }
+    __syncthreads();
+    // U^{-1}
+    for (int e = tid; e < N * N; e += DIAG_THREADS) x[e / N][e % N] = (e / N == e % N) ? 1.f : 0.f;
+    __syncthreads();
+    for (int j = N - 1; j >= 0; --j) {
+        const float d = a[j][j];
+        for (int c = j + tid; c < N; c += DIAG_THREADS) x[j][c] = x[j][c] / d;
+        __syncthreads();
+        for (int e = tid; e < j * (N - j); e += DIAG_THREADS) {
+            const int i = e % j, c = j + e / j;
+            x[i][c] = fmaf(-a[i][j], x[j][c], x[i][c]);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e % N, c = e / N;
+        J.Ui[r + c * N] = x[r][c];
+        put_split(J.UiRh, J.UiRl, (long long)r * N + c, x[r][c]);
+        put_split(J.UiCh, J.UiCl, (long long)c * N + r, x[r][c]);
+    }
+}
+
+constexpr int DIAG_SMEM = 2 * MX_NB * DP * (int)sizeof(float);
+
+void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
+    static bool attr = false;
+    if (!attr) {
+        CUDA_CHECK(cudaFuncSetAttribute(diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM));
+        attr = true;
+    }
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        DiagArgs a;
+        a.flag = cx.flag;
+        const int n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        for (int k = 0; k < n; ++k) a.j[k] = jobs[i0 + k];
+        LAUNCH(diag_kernel, n, DIAG_THREADS, DIAG_SMEM, cx.st, a);
+    }
+}
+
+// ---------------------------------------------------------------- views
+// Left operand: rows [r0, r0 + nr) x columns [c0, c0 + nc) of a row-major split copy.
+SplitMat rview(bf16* h, bf16* l, long long ld, int r0, int c0, int nr, int nc) {
+    const long long o = (long long)r0 * ld + c0;
+    return {h + o, l + o, nr, nc, ld};
+}
+// Right operand: rows [r0, r0 + nr) (= K) x columns [c0, c0 + nc) (= N) of a
+// column-major split copy.
+SplitMat cview(bf16* h, bf16* l, long long ld, int r0, int c0, int nr, int nc) {
+    const long long o = (long long)c0 * ld + r0;
+    return {h + o, l + o, nc, nr, ld};
+}
+
+// A target being solved in place: FP32 column-major X plus split copies.
+struct Target {
+    float* X;
+    long long ldx;
+    bf16 *Ch, *Cl;  // column-major split (required)
+    long long ldc;
+    bf16 *Rh, *Rl;  // row-major split (optional)
+    long long ldr;
+};
+
+void run(std::vector<TcProblem>& P, std::vector<TcOperands>& O, const MixedCtx& cx) {
+    if (!P.empty()) tc_gemm(P, O, cx.err, cx.flag, cx.st);
+    P.clear();
+    O.clear();
+}
+
+// TRSM with the unit-lower (lower = true) or upper factor of every member on
+// rows [k0, k0 + w), columns [j0, j0 + nc) of its target.
+void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool lower, int k0, int w, int j0,
+          const std::vector<int>& ncols, const MixedCtx& cx) {
+    std::vector<TcProblem> P;
+    std::vector<TcOperands> O;
+    if (w == MX_NB) {
+        // leaf: B -> split (column-major), X = inv_b * B, keep the split copies equal to X
+        std::vector<ConvJob> cj;
+        for (size_t m = 0; m < g.size(); ++m) {
+            if (ncols[m] <= 0) continue;
+            const Target& t = T[m];
+            cj.push_back({t.X + k0 + (long long)j0 * t.ldx, 1, t.ldx, MX_NB, ncols[m], t.Ch + k0 + (long long)j0 * t.ldc,
+                          t.Cl + k0 + (long long)j0 * t.ldc, 1, t.ldc});
+        }
+        convert_group(cj, cx.st);
+        const int b = k0 / MX_NB;
+        for (size_t m = 0; m < g.size(); ++m) {
+            if (ncols[m] <= 0) continue;
+            MixedLU& L = *g[m];
+            const Target& t = T[m];
+            const long long bo = (long long)b * MX_NB * MX_NB;
+            TcProblem p;
+            p.M = MX_NB; p.N = ncols[m]; p.K = MX_NB;
+            p.alpha = 1.f; p.beta = 0.f;
+            p.C = t.X + k0 + (long long)j0 * t.ldx; p.c_rs = 1; p.c_cs = t.ldx;
+            p.O_hi = t.Ch + k0 + (long long)j0 * t.ldc; p.O_lo = t.Cl + k0 + (long long)j0 * t.ldc;
+            p.o_rs = 1; p.o_cs = t.ldc;
+            if (t.Rh) {
+                p.P_hi = t.Rh + (long long)k0 * t.ldr + j0; p.P_lo = t.Rl + (long long)k0 * t.ldr + j0;
+                p.p_rs = t.ldr; p.p_cs = 1;
+            }
+            TcOperands o;
+            o.A = lower ? SplitMat{L.LiRh.get() + bo, L.LiRl.get() + bo, MX_NB, MX_NB, MX_NB}
+                        : SplitMat{L.UiRh.get() + bo, L.UiRl.get() + bo, MX_NB, MX_NB, MX_NB};
+            o.B = cview(t.Ch, t.Cl, t.ldc, k0, j0, MX_NB, ncols[m]);
+            P.push_back(p);
+            O.push_back(o);
+        }
+        run(P, O, cx);
+        return;
+    }
+    const int w1 = std::max(MX_NB, (w / MX_NB / 2) * MX_NB), w2 = w - w1;
+    // lower: first half solves, then updates the second; upper: the reverse
+    const int ka = lower ? k0 : k0 + w1, wa = lower ? w1 : w2;  // solved first
+    const int kb = lower ? k0 + w1 : k0, wb = lower ? w2 : w1;  // updated, solved second
+    trsm(g, T, lower, ka, wa, j0, ncols, cx);
+    for (size_t m = 0; m < g.size(); ++m) {
+        if (ncols[m] <= 0) continue;
+        MixedLU& L = *g[m];
+        const Target& t = T[m];
+        TcProblem p;
+        p.M = wb; p.N = ncols[m]; p.K = wa;
+        p.alpha = -1.f; p.beta = 1.f;
+        p.C = t.X + kb + (long long)j0 * t.ldx; p.c_rs = 1; p.c_cs = t.ldx;
+        TcOperands o;
+        o.A = rview(L.Rh.get(), L.Rl.get(), L.n, kb, ka, wb, wa);  // factor block (rows kb, columns ka)
+        o.B = cview(t.Ch, t.Cl, t.ldc, ka, j0, wa, ncols[m]);       // solved rows of X
+        P.push_back(p);
+        O.push_back(o);
+    }
+    run(P, O, cx);
+    trsm(g, T, lower, kb, wb, j0, ncols, cx);
+}
+
+void leaf(const std::vector<MixedLU*>& g, int c0, const MixedCtx& cx) {
+    std::vector<DiagJob> dj;
+    const int b = c0 / MX_NB;
+    for (MixedLU* L : g) {
+        const long long bo = (long long)b * MX_NB * MX_NB;
+        dj.push_back({L->A.get() + c0 + (long long)c0 * L->n, L->n, L->Li.get() + bo, L->Ui.get() + bo,
+                      L->LiRh.get() + bo, L->LiRl.get() + bo, L->UiRh.get() + bo, L->UiRl.get() + bo,
+                      L->UiCh.get() + bo, L->UiCl.get() + bo});
+    }
+    diag_group(dj, cx);
+    const int n = g[0]->n, rows = n - c0 - MX_NB;
+    if (rows <= 0) return;
+    // L21 = A21 U11^{-1}: A21 -> row-major split, GEMM writes L21 (FP32 + row-major split)
+    std::vector<ConvJob> cj;
+    for (MixedLU* L : g) {
+        const long long ld = L->n;
+        cj.push_back({L->A.get() + (c0 + MX_NB) + (long long)c0 * ld, 1, ld, rows, MX_NB,
+                      L->Rh.get() + (long long)(c0 + MX_NB) * ld + c0, L->Rl.get() + (long long)(c0 + MX_NB) * ld + c0,
+                      ld, 1});
+    }
+    convert_group(cj, cx.st);
+    std::vector<TcProblem> P;
+    std::vector<TcOperands> O;
+    for (MixedLU* L : g) {
+        const long long ld = L->n, bo = (long long)b * MX_NB * MX_NB;
+        TcProblem p;
+        p.M = rows; p.N = MX_NB; p.K = MX_NB;
+        p.alpha = 1.f; p.beta = 0.f;
+        p.C = L->A.get() + (c0 + MX_NB) + (long long)c0 * ld; p.c_rs = 1; p.c_cs = ld;
+        p.O_hi = L->Rh.get() + (long long)(c0 + MX_NB) * ld + c0;
+        p.O_lo = L->Rl.get() + (long long)(c0 + MX_NB) * ld + c0;
+        p.o_rs = ld; p.o_cs = 1;
+        p.check_unit = 1;
+        TcOperands o;
+        o.A = rview(L->Rh.get(), L->Rl.get(), ld, c0 + MX_NB, c0, rows, MX_NB);
+        o.B = SplitMat{L->UiCh.get() + bo, L->UiCl.get() + bo, MX_NB, MX_NB, MX_NB};
+        P.push_back(p);
+        O.push_back(o);
+    }
+    run(P, O, cx);
+}
+
+void lu_rec(const std::vector<MixedLU*>& g, int c0, int w, const MixedCtx& cx) {
+    if (w == MX_NB) {
+        leaf(g, c0, cx);
+        return;
+    }
+    const int w1 = std::max(MX_NB, (w / MX_NB / 2) * MX_NB), w2 = w - w1;
+    const int n = g[0]->n;
+    lu_rec(g, c0, w1, cx);
+    // U12 = L11^{-1} A12 on rows [c0, c0 + w1), columns [c0 + w1, c0 + w)
+    std::vector<Target> T;
+    std::vector<int> nc;
+    for (MixedLU* L : g) {
+        T.push_back({L->A.get(), L->n, L->Ch.get(), L->Cl.get(), L->n, L->Rh.get(), L->Rl.get(), L->n});
+        nc.push_back(w2);
+    }
+    trsm(g, T, true, c0, w1, c0 + w1, nc, cx);
+    // A22 -= L21 U12 (rows [c0 + w1, n), columns [c0 + w1, c0 + w), K = w1)
+    std::vector<TcProblem> P;
+    std::vector<TcOperands> O;
+    const int rows = n - c0 - w1;
+    for (MixedLU* L : g) {
+        const long long ld = L->n;
+        TcProblem p;
+        p.M = rows; p.N = w2; p.K = w1;
+        p.alpha = -1.f; p.beta = 1.f;
+        p.C = L->A.get() + (c0 + w1) + (long long)(c0 + w1) * ld; p.c_rs = 1; p.c_cs = ld;
+        TcOperands o;
+        o.A = rview(L->Rh.get(), L->Rl.get(), ld, c0 + w1, c0, rows, w1);
+        o.B = cview(L->Ch.get(), L->Cl.get(), ld, c0, c0 + w1, w1, w2);
+        P.push_back(p);
+        O.push_back(o);
+    }
+    run(P, O, cx);
+    lu_rec(g, c0 + w1, w2, cx);
+}
+
+}  // namespace
+
+void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
+    if (jobs.empty()) return;
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        ConvArgs a;
+        a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        long long mx = 0;
+        for (int k = 0; k < a.n; ++k) {
+            a.j[k] = jobs[i0 + k];
+            mx = std::max(mx, (long long)a.j[k].rows * a.j[k].cols);
+        }
+        if (mx == 0) continue;
+        const int gx = (int)std::min<long long>(ceil_div(mx, 256), 2048);
+        LAUNCH(conv_kernel, dim3(gx, (unsigned)a.n), 256, 0, st, a);
+    }
+}
+
+void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx) {
+    if (g.empty()) return;
+    const int n = g[0]->n;
+    for (MixedLU* L : g)
+        if (L->n != n) fail(SQBEM_ERR_ARG, "mixed_lu_factor: group members differ in size");
+    lu_rec(g, 0, n, cx);
+}
+
+void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx) {
+    if (g.empty()) return;
+    std::vector<Target> T;
+    std::vector<int> nc;
+    int maxc = 0;
+    for (size_t m = 0; m < g.size(); ++m) {
+        const Rhs& r = rhs[m];
+        T.push_back({r.X, r.ldx, r.Sh, r.Sl, r.lds, r.Rh, r.Rl, r.ldr});
+        nc.push_back(r.nrhs);
+        maxc = std::max(maxc, r.nrhs);
+    }
+    if (maxc == 0) return;
+    const int n = g[0]->n;
+    trsm(g, T, true, 0, n, 0, nc, cx);
+    trsm(g, T, false, 0, n, 0, nc, cx);
+}
+
+}  // namespace sqbem

@@ -1,0 +1,587 @@
+// mixed_solver.cu -- the SQBEM_MIXED swimmer path over groups of instances.
+//
+// Build (per group): FP32 assembly of every block (FP64 relative vectors, FP64
+// 448-point and self integrals), LU(T) and Y = T^{-1}[B | Ct] on the tensor
+// cores, G = [E | Cs] - D Y, LU(G_s), Z = G_s^{-1} G_c, S6 = F Z inverted in
+// FP64 on the host (6 x 6).
+// Solve: iterative refinement of the full system in FP64 (see mixed_solver.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "assemble.cuh"
+#include "common.cuh"
+#include "matvec.cuh"
+#include "mixed.cuh"
+#include "mixed_solver.cuh"
+#include "solver.cuh"
+
+namespace sqbem {
+
+namespace {
+
+__global__ void pad_identity_kernel(float* A, long long ld, int n0, int n1) {
+    const int i = n0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n1) A[i + (long long)i * ld] = 1.f;
+}
+
+void pad_identity(float* A, long long ld, int n0, int n1, cudaStream_t st) {
+    if (n1 > n0) LAUNCH(pad_identity_kernel, ceil_div(n1 - n0, 128), 128, 0, st, A, ld, n0, n1);
+}
+
+BlockJob<float> fjob(const DevPanels& tgt, const DevPanels& src, bool same, double mu, float* S, long long lds,
+                     float* D, long long ldd) {
+    BlockJob<float> j;
+    j.tgt = tgt.cent.get();
+    j.nT = tgt.P;
+    j.src = src.rec.get();
+    j.nS = src.P;
+    j.same_mesh = same ? 1 : 0;
+    j.S = S;
+    j.s_rs = 1;
+    j.s_cs = lds;
+    j.D = D;
+    j.d_rs = 1;
+    j.d_cs = ldd;
+    j.sscale = 1.0 / (EIGHT_PI * mu);
+    j.dscale = -1.0 / EIGHT_PI;
+    return j;
+}
+
+int cap_pairs(int a, int b) { return (int)std::min<long long>((long long)a * b, 64LL << 20); }
+
+int read_int(const int* d, cudaStream_t st) {
+    int h = 0;
+    CUDA_CHECK(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    count_d2h(sizeof(int));
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    return h;
+}
+
+void check_ctx(const MixedCtx& cx, const char* what) {
+    if (read_int(cx.err, cx.st)) fail(SQBEM_ERR_TIMEOUT, "%s: a bounded wait in the tensor-core GEMM expired", what);
+    const int f = read_int(cx.flag, cx.st);
+    if (f & 2) fail(SQBEM_ERR_SINGULAR, "%s failed: zero pivot", what);
+    if (f & 1)
+        fail(SQBEM_ERR_SINGULAR, "%s: partial pivoting would exchange rows; the mixed LU does not pivot", what);
+}
+
+// 6 x 6 inverse by Gauss-Jordan with partial pivoting (FP64, host)
+bool invert6(const double* A, double* Ai) {
+    double a[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            a[i][j] = A[i + 6 * j];
+            a[i][6 + j] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 6; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 6; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
+        if (!(std::fabs(a[p][c]) > 0)) return false;
+        if (p != c)
+            for (int j = 0; j < 12; ++j) std::swap(a[p][j], a[c][j]);
+        const double d = a[c][c];
+        for (int j = 0; j < 12; ++j) a[c][j] /= d;
+        for (int r = 0; r < 6; ++r)
+            if (r != c) {
+                const double f = a[r][c];
+                for (int j = 0; j < 12; ++j) a[r][j] -= f * a[c][j];
+            }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) Ai[i + 6 * j] = a[i][6 + j];
+    return true;
+}
+
+CopyJob cp32_64(const float* s, long long lds, double* d, long long ldd, int rows, int cols) {
+    CopyJob j;
+    j.s32 = s; j.lds = lds; j.d64 = d; j.ldd = ldd; j.rows = rows; j.cols = cols;
+    return j;
+}
+CopyJob cp64_32(const double* s, long long lds, float* d, long long ldd, int rows, int cols) {
+    CopyJob j;
+    j.s64 = s; j.lds = lds; j.d32 = d; j.ldd = ldd; j.rows = rows; j.cols = cols;
+    return j;
+}
+CopyJob cp32_32(const float* s, long long lds, float* d, long long ldd, int rows, int cols) {
+    CopyJob j;
+    j.s32 = s; j.lds = lds; j.d32 = d; j.ldd = ldd; j.rows = rows; j.cols = cols;
+    return j;
+}
+CopyJob cp64(const double* s, long long lds, double* d, long long ldd, int rows, int cols, double alpha = 1,
+             double beta = 0) {
+    CopyJob j;
+    j.s64 = s; j.lds = lds; j.d64 = d; j.ldd = ldd; j.rows = rows; j.cols = cols; j.alpha = alpha; j.beta = beta;
+    return j;
+}
+MvJob mv32(const float* A, long long lda, int m, int n, const double* x, long long ldx, int r, double* y,
+           long long ldy, double alpha, double beta) {
+    MvJob j;
+    j.A32 = A; j.lda = lda; j.m = m; j.n = n; j.x = x; j.ldx = ldx; j.r = r; j.y = y; j.ldy = ldy;
+    j.alpha = alpha; j.beta = beta;
+    return j;
+}
+MvJob mv64(const double* A, long long lda, int m, int n, const double* x, long long ldx, int r, double* y,
+           long long ldy, double alpha, double beta) {
+    MvJob j = mv32(nullptr, lda, m, n, x, ldx, r, y, ldy, alpha, beta);
+    j.A64 = A;
+    return j;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- tubes
+void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx) {
+    std::vector<MixedLU*> lus;
+    std::vector<CopyJob> cj;
+    for (sqbem_tube* t : tubes) {
+        MixedTube& M = t->mt;
+        M.nt = 3 * t->Nt;
+        M.lu.alloc(M.nt, cx.st);
+        const int np = M.lu.n;
+        M.lu.A.zero();
+        auto job = fjob(t->panels, t->panels, true, t->mu, M.lu.A.get(), np, nullptr, 0);
+        assemble_block(job, cap_pairs(t->Nt, t->Nt), cx.st, true);
+        deflate<float>(M.lu.A.get(), 1, np, t->panels, t->mu, cx.st);
+        pad_identity(M.lu.A.get(), np, M.nt, np, cx.st);
+        M.T.alloc((size_t)M.nt * M.nt, cx.st);
+        cj.push_back(cp32_32(M.lu.A.get(), np, M.T.get(), M.nt, M.nt, M.nt));
+        lus.push_back(&M.lu);
+    }
+    copy_group(cj, cx.st);
+    mixed_lu_factor(lus, cx);
+    check_ctx(cx, "dgetrf (mixed tube factor)");
+}
+
+// ---------------------------------------------------------------- swimmers
+void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx) {
+    if (sw.empty()) return;
+    const bool bounded = sw[0]->tube != nullptr;
+    std::vector<CopyJob> cj;
+    std::vector<MvJob> mj;
+    std::vector<DevBuf<double>> tmp;
+    tmp.reserve(2 * sw.size());
+    for (sqbem_swimmer* s : sw) {
+        MixedSwimmer& M = s->mx;
+        const int Ns = s->Ns, Nt = s->Nt;
+        M.ns = 3 * Ns;
+        M.nt = 3 * Nt;
+        M.nc = M.ns + 6;
+        const int ns = M.ns, nt = M.nt;
+        M.E.alloc((size_t)ns * ns, cx.st);
+        M.AuBs.alloc((size_t)ns * ns, cx.st);
+        DevBuf<double> rsum((size_t)ns * 3, cx.st);
+        rsum.zero();
+        if (bounded) {
+            M.B.alloc((size_t)nt * ns, cx.st);
+            M.AuBt.alloc((size_t)nt * ns, cx.st);
+            auto j1 = fjob(s->tube->panels, s->panels, false, s->mu, M.B.get(), nt, M.AuBt.get(), nt);
+            assemble_block(j1, cap_pairs(Nt, Ns), cx.st, true);
+            M.D.alloc((size_t)ns * nt, cx.st);
+            DevBuf<float> Dt((size_t)ns * nt, cx.st);
+            auto j2 = fjob(s->panels, s->tube->panels, false, s->mu, M.D.get(), ns, Dt.get(), ns);
+            assemble_block(j2, cap_pairs(Ns, Nt), cx.st, true);
+            add_rowsums<float>(Dt.get(), 1, ns, ns, Nt, rsum.get(), cx.st);
+        }
+        auto j3 = fjob(s->panels, s->panels, true, s->mu, M.E.get(), ns, M.AuBs.get(), ns);
+        assemble_block(j3, cap_pairs(Ns, Ns), cx.st, true);
+        add_rowsums<float>(M.AuBs.get(), 1, ns, ns, Ns, rsum.get(), cx.st);
+        diag_complete<float>(M.AuBs.get(), 1, ns, Ns, rsum.get(), bounded ? 0.0 : 1.0, nullptr, cx.st);
+        deflate<float>(M.E.get(), 1, ns, s->panels, s->mu, cx.st);
+        // rigid-body map, C = A_u K (accumulated in FP64, stored FP32)
+        const auto Kh = rigid_map(s->host_panels, s->xc);
+        M.K.alloc(Kh.size(), cx.st);
+        M.K.upload(Kh.data(), Kh.size());
+        M.Cs.alloc((size_t)ns * 6, cx.st);
+        tmp.emplace_back((size_t)ns * 6, cx.st);
+        mj.push_back(mv32(M.AuBs.get(), ns, ns, ns, M.K.get(), ns, 6, tmp.back().get(), ns, 1.0, 0.0));
+        cj.push_back(cp64_32(tmp.back().get(), ns, M.Cs.get(), ns, ns, 6));
+        if (bounded) {
+            M.Ct.alloc((size_t)nt * 6, cx.st);
+            tmp.emplace_back((size_t)nt * 6, cx.st);
+            mj.push_back(mv32(M.AuBt.get(), nt, nt, ns, M.K.get(), ns, 6, tmp.back().get(), nt, 1.0, 0.0));
+            cj.push_back(cp64_32(tmp.back().get(), nt, M.Ct.get(), nt, nt, 6));
+        }
+        const auto F = constraint_rows(s->host_panels, s->xc, 1.0);
+        M.F.alloc(F.size(), cx.st);
+        M.F.upload(F.data(), F.size());
+    }
+    matvec_group(mj, cx.st);
+    copy_group(cj, cx.st);
+    cj.clear();
+    mj.clear();
+    tmp.clear();
+
+    // Schur complement: Y = T^{-1} [B | Ct];  [G_s | G_c] = [E | Cs] - D Y
+    if (bounded) {
+        std::vector<MixedLU*> tl;
+        std::vector<Rhs> rh;
+        for (sqbem_swimmer* s : sw) {
+            MixedSwimmer& M = s->mx;
+            MixedLU& L = const_cast<sqbem_tube*>(s->tube)->mt.lu;
+            const int ntp = L.n;
+            M.Y.alloc((size_t)ntp * M.nc, cx.st);
+            M.Y.zero();
+            M.Yh.alloc((size_t)ntp * M.nc, cx.st);
+            M.Yl.alloc((size_t)ntp * M.nc, cx.st);
+            cj.push_back(cp32_32(M.B.get(), M.nt, M.Y.get(), ntp, M.nt, M.ns));
+            cj.push_back(cp32_32(M.Ct.get(), M.nt, M.Y.get() + (size_t)ntp * M.ns, ntp, M.nt, 6));
+            tl.push_back(&L);
+            Rhs r;
+            r.X = M.Y.get(); r.ldx = ntp; r.nrhs = M.nc; r.Sh = M.Yh.get(); r.Sl = M.Yl.get(); r.lds = ntp;
+            rh.push_back(r);
+        }
+        copy_group(cj, cx.st);
+        cj.clear();
+        mixed_lu_solve(tl, rh, cx);
+    }
+    std::vector<MixedLU*> gl;
+    std::vector<ConvJob> conv;
+    for (sqbem_swimmer* s : sw) {
+        MixedSwimmer& M = s->mx;
+        M.G.alloc(M.ns, cx.st);
+        const int nsp = M.G.n;
+        M.G.A.zero();
+        cj.push_back(cp32_32(M.E.get(), M.ns, M.G.A.get(), nsp, M.ns, M.ns));
+        pad_identity(M.G.A.get(), nsp, M.ns, nsp, cx.st);
+        M.Gc.alloc((size_t)M.ns * 6, cx.st);
+        cj.push_back(cp32_32(M.Cs.get(), M.ns, M.Gc.get(), M.ns, M.ns, 6));
+        if (bounded) {
+            const int ntp = s->tube->mt.lu.n;
+            M.Dh.alloc((size_t)M.ns * ntp, cx.st);
+            M.Dl.alloc((size_t)M.ns * ntp, cx.st);
+            M.Dh.zero();
+            M.Dl.zero();
+            conv.push_back({M.D.get(), 1, M.ns, M.ns, M.nt, M.Dh.get(), M.Dl.get(), ntp, 1});
+        }
+        gl.push_back(&M.G);
+    }
+    copy_group(cj, cx.st);
+    cj.clear();
+    if (bounded) {
+        convert_group(conv, cx.st);
+        std::vector<TcProblem> P;
+        std::vector<TcOperands> O;
+        for (sqbem_swimmer* s : sw) {
+            MixedSwimmer& M = s->mx;
+            const int ntp = s->tube->mt.lu.n, nsp = M.G.n;
+            TcOperands o;
+            o.A = {M.Dh.get(), M.Dl.get(), M.ns, ntp, ntp};
+            TcProblem p;
+            p.M = M.ns; p.N = M.ns; p.K = ntp; p.alpha = -1.f; p.beta = 1.f;
+            p.C = M.G.A.get(); p.c_rs = 1; p.c_cs = nsp;
+            o.B = {M.Yh.get(), M.Yl.get(), M.ns, ntp, ntp};
+            P.push_back(p);
+            O.push_back(o);
+            TcProblem q = p;
+            q.N = 6;
+            q.C = M.Gc.get(); q.c_cs = M.ns;
+            TcOperands o2 = o;
+            o2.B = {M.Yh.get() + (size_t)ntp * M.ns, M.Yl.get() + (size_t)ntp * M.ns, 6, ntp, ntp};
+            P.push_back(q);
+            O.push_back(o2);
+        }
+        tc_gemm(P, O, cx.err, nullptr, cx.st);
+    }
+    mixed_lu_factor(gl, cx);
+    // Z = G_s^{-1} G_c
+    std::vector<Rhs> zr;
+    for (sqbem_swimmer* s : sw) {
+        MixedSwimmer& M = s->mx;
+        const int nsp = M.G.n;
+        M.Z.alloc((size_t)nsp * 6, cx.st);
+        M.Z.zero();
+        M.Zh.alloc((size_t)nsp * 6, cx.st);
+        M.Zl.alloc((size_t)nsp * 6, cx.st);
+        cj.push_back(cp32_32(M.Gc.get(), M.ns, M.Z.get(), nsp, M.ns, 6));
+        Rhs r;
+        r.X = M.Z.get(); r.ldx = nsp; r.nrhs = 6; r.Sh = M.Zh.get(); r.Sl = M.Zl.get(); r.lds = nsp;
+        zr.push_back(r);
+    }
+    copy_group(cj, cx.st);
+    cj.clear();
+    mixed_lu_solve(gl, zr, cx);
+    // S6 = F Z in FP64, inverted on the host
+    DevBuf<double> s6((size_t)36 * sw.size(), cx.st);
+    for (size_t k = 0; k < sw.size(); ++k) {
+        MixedSwimmer& M = sw[k]->mx;
+        M.Z64.alloc((size_t)M.ns * 6, cx.st);
+        cj.push_back(cp32_64(M.Z.get(), M.G.n, M.Z64.get(), M.ns, M.ns, 6));
+        mj.push_back(mv64(M.F.get(), 6, 6, M.ns, M.Z64.get(), M.ns, 6, s6.get() + 36 * k, 6, 1.0, 0.0));
+    }
+    copy_group(cj, cx.st);
+    matvec_group(mj, cx.st);
+    std::vector<double> h6(36 * sw.size());
+    s6.download(h6.data(), h6.size());
+    check_ctx(cx, "dgetrf (mixed Schur factor)");
+    for (size_t k = 0; k < sw.size(); ++k) {
+        double inv[36];
+        if (!invert6(h6.data() + 36 * k, inv)) fail(SQBEM_ERR_SINGULAR, "dgesv failed (rigid-body 6 x 6 system)");
+        MixedSwimmer& M = sw[k]->mx;
+        M.S6i.alloc(36, cx.st);
+        M.S6i.upload(inv, 36);
+    }
+    // the assembly-only buffers are no longer needed
+    for (sqbem_swimmer* s : sw) {
+        s->mx.Dh.release();
+        s->mx.Dl.release();
+        s->mx.Zh.release();
+        s->mx.Zl.release();
+    }
+}
+
+// ---------------------------------------------------------------- refinement
+void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const std::vector<const double*>& in, int r,
+                 const std::vector<double*>& xs, const MixedCtx& cx, int* iterations, double* residual) {
+    const size_t G = sw.size();
+    if (G == 0) return;
+    const bool bounded = sw[0]->tube != nullptr;
+    struct Work {
+        DevBuf<double> bt, bs, rt, rs, rc, rsp, yt64, v64, tmp6, dsw, dt, nrm;
+        DevBuf<float> yt32, v32;
+        DevBuf<bf16> yth, ytl, vh, vl;
+    };
+    std::vector<Work> W(G);
+    std::vector<MvJob> mj;
+    std::vector<CopyJob> cj;
+    for (size_t k = 0; k < G; ++k) {
+        MixedSwimmer& M = sw[k]->mx;
+        Work& w = W[k];
+        const int nt = M.nt, ns = M.ns, nc = M.nc;
+        const int ntp = bounded ? sw[k]->tube->mt.lu.n : 0, nsp = M.G.n;
+        const size_t ntr = (size_t)std::max(nt, 1) * r;
+        w.bt.alloc(ntr, cx.st); w.rt.alloc(ntr, cx.st); w.dt.alloc(ntr, cx.st); w.yt64.alloc(ntr, cx.st);
+        w.bs.alloc((size_t)ns * r, cx.st); w.rs.alloc((size_t)ns * r, cx.st);
+        w.rsp.alloc((size_t)ns * r, cx.st); w.v64.alloc((size_t)ns * r, cx.st);
+        w.rc.alloc((size_t)6 * r, cx.st); w.tmp6.alloc((size_t)6 * r, cx.st);
+        w.dsw.alloc((size_t)nc * r, cx.st); w.nrm.alloc((size_t)4 * r, cx.st);
+        if (bounded) {
+            w.yt32.alloc((size_t)ntp * r, cx.st);
+            w.yth.alloc((size_t)ntp * r, cx.st);
+            w.ytl.alloc((size_t)ntp * r, cx.st);
+        }
+        w.v32.alloc((size_t)nsp * r, cx.st); w.vh.alloc((size_t)nsp * r, cx.st); w.vl.alloc((size_t)nsp * r, cx.st);
+        CUDA_CHECK(cudaMemsetAsync(xs[k], 0, sizeof(double) * (size_t)(nt + nc) * r, cx.st));
+        CUDA_CHECK(cudaMemsetAsync(w.rc.get(), 0, sizeof(double) * 6 * r, cx.st));
+        if (prescribed) {
+            // rigid motion given: b = 0, x_w = w fixed (swimmer.hpp:142-153)
+            CUDA_CHECK(cudaMemsetAsync(w.bt.get(), 0, sizeof(double) * ntr, cx.st));
+            CUDA_CHECK(cudaMemsetAsync(w.bs.get(), 0, sizeof(double) * ns * r, cx.st));
+            cj.push_back(cp64(in[k], 6, xs[k] + nt + ns, nt + nc, 6, r));
+        } else {
+            // slip: b_t = -A_uBt u, b_s = -A_uBs u  (swimmer.hpp:256-269)
+            if (bounded) mj.push_back(mv32(M.AuBt.get(), nt, nt, ns, in[k], ns, r, w.bt.get(), nt, -1.0, 0.0));
+            mj.push_back(mv32(M.AuBs.get(), ns, ns, ns, in[k], ns, r, w.bs.get(), ns, -1.0, 0.0));
+        }
+    }
+    matvec_group(mj, cx.st);
+    mj.clear();
+    copy_group(cj, cx.st);
+    cj.clear();
+
+    // r = b - A x (FP64), in three rounds that write r_t, r_s, r_c at most once each
+    auto compute_residual = [&]() {
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            if (bounded) cj.push_back(cp64(W[k].bt.get(), M.nt, W[k].rt.get(), M.nt, M.nt, r));
+            cj.push_back(cp64(W[k].bs.get(), M.ns, W[k].rs.get(), M.ns, M.ns, r));
+        }
+        copy_group(cj, cx.st);
+        cj.clear();
+        for (int round = 0; round < 3; ++round) {
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const long long ldx = M.nt + M.nc;
+                const double* xt = xs[k];
+                const double* xsp = xs[k] + M.nt;
+                const double* xw = xs[k] + M.nt + M.ns;
+                double* rt = W[k].rt.get();
+                double* rs = W[k].rs.get();
+                if (round == 0) {
+                    if (bounded) {
+                        mj.push_back(mv32(sw[k]->tube->mt.T.get(), M.nt, M.nt, M.nt, xt, ldx, r, rt, M.nt, -1.0, 1.0));
+                        mj.push_back(mv32(M.D.get(), M.ns, M.ns, M.nt, xt, ldx, r, rs, M.ns, -1.0, 1.0));
+                    }
+                    if (!prescribed)
+                        mj.push_back(mv64(M.F.get(), 6, 6, M.ns, xsp, ldx, r, W[k].rc.get(), 6, -1.0, 0.0));
+                } else if (round == 1) {
+                    if (bounded) mj.push_back(mv32(M.B.get(), M.nt, M.nt, M.ns, xsp, ldx, r, rt, M.nt, -1.0, 1.0));
+                    mj.push_back(mv32(M.E.get(), M.ns, M.ns, M.ns, xsp, ldx, r, rs, M.ns, -1.0, 1.0));
+                } else {
+                    if (bounded) mj.push_back(mv32(M.Ct.get(), M.nt, M.nt, 6, xw, ldx, r, rt, M.nt, -1.0, 1.0));
+                    mj.push_back(mv32(M.Cs.get(), M.ns, M.ns, 6, xw, ldx, r, rs, M.ns, -1.0, 1.0));
+                }
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+        }
+    };
+    // |r|^2 per right-hand side (tube, sphere and constraint rows together)
+    auto norms = [&]() {
+        std::vector<NormJob> nj;
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            Work& w = W[k];
+            CUDA_CHECK(cudaMemsetAsync(w.nrm.get(), 0, sizeof(double) * 4 * r, cx.st));
+            if (bounded) nj.push_back({w.rt.get(), M.nt, M.nt, r, w.nrm.get()});
+            nj.push_back({w.rs.get(), M.ns, M.ns, r, w.nrm.get() + r});
+            nj.push_back({w.rc.get(), 6, 6, r, w.nrm.get() + 2 * r});
+        }
+        sumsq_group(nj, cx.st);
+        std::vector<double> h(4 * r * G);
+        for (size_t k = 0; k < G; ++k) W[k].nrm.download(h.data() + 4 * r * k, 4 * r);
+        CUDA_CHECK(cudaStreamSynchronize(cx.st));
+        std::vector<double> out(G * r);
+        for (size_t k = 0; k < G; ++k)
+            for (int c = 0; c < r; ++c) out[k * r + c] = h[4 * r * k + c] + h[4 * r * k + r + c] + h[4 * r * k + 2 * r + c];
+        return out;
+    };
+    compute_residual();
+    const std::vector<double> r0 = norms();
+    int it = 0;
+    double worst = 0;
+    for (size_t k = 0; k < G * r; ++k) worst = std::max(worst, r0[k] > 0 ? 1.0 : 0.0);
+    for (it = 1; it <= REFINE_MAX_IT && worst > REFINE_TOL; ++it) {
+        // (a) y_t = T^{-1} r_t   (b) r_s' = r_s - D y_t
+        if (bounded) {
+            std::vector<MixedLU*> tl;
+            std::vector<Rhs> rh;
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                Work& w = W[k];
+                MixedLU& L = const_cast<sqbem_tube*>(sw[k]->tube)->mt.lu;
+                CUDA_CHECK(cudaMemsetAsync(w.yt32.get(), 0, sizeof(float) * (size_t)L.n * r, cx.st));
+                cj.push_back(cp64_32(w.rt.get(), M.nt, w.yt32.get(), L.n, M.nt, r));
+                tl.push_back(&L);
+                Rhs x;
+                x.X = w.yt32.get(); x.ldx = L.n; x.nrhs = r; x.Sh = w.yth.get(); x.Sl = w.ytl.get(); x.lds = L.n;
+                rh.push_back(x);
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+            mixed_lu_solve(tl, rh, cx);
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const int ntp = sw[k]->tube->mt.lu.n;
+                cj.push_back(cp32_64(W[k].yt32.get(), ntp, W[k].yt64.get(), M.nt, M.nt, r));
+                cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                mj.push_back(mv32(M.D.get(), M.ns, M.ns, M.nt, W[k].yt64.get(), M.nt, r, W[k].rsp.get(), M.ns, -1.0, 1.0));
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+        } else {
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+        }
+        // (c) v = G_s^{-1} r_s'
+        {
+            std::vector<MixedLU*> gl;
+            std::vector<Rhs> rh;
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                Work& w = W[k];
+                CUDA_CHECK(cudaMemsetAsync(w.v32.get(), 0, sizeof(float) * (size_t)M.G.n * r, cx.st));
+                cj.push_back(cp64_32(w.rsp.get(), M.ns, w.v32.get(), M.G.n, M.ns, r));
+                gl.push_back(&M.G);
+                Rhs x;
+                x.X = w.v32.get(); x.ldx = M.G.n; x.nrhs = r; x.Sh = w.vh.get(); x.Sl = w.vl.get(); x.lds = M.G.n;
+                rh.push_back(x);
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+            mixed_lu_solve(gl, rh, cx);
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                cj.push_back(cp32_64(W[k].v32.get(), M.G.n, W[k].v64.get(), M.ns, M.ns, r));
+                cj.push_back(cp32_64(W[k].v32.get(), M.G.n, W[k].dsw.get(), M.nc, M.ns, r));
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+        }
+        if (prescribed) {
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                for (int c = 0; c < r; ++c)
+                    CUDA_CHECK(cudaMemsetAsync(W[k].dsw.get() + M.ns + (size_t)c * M.nc, 0, 6 * sizeof(double), cx.st));
+            }
+        } else {
+            // (d) dw = S6^{-1} (F v - r_c)   (e) ds = v - Z dw
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                mj.push_back(mv64(M.F.get(), 6, 6, M.ns, W[k].v64.get(), M.ns, r, W[k].tmp6.get(), 6, 1.0, 0.0));
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+            for (size_t k = 0; k < G; ++k) cj.push_back(cp64(W[k].rc.get(), 6, W[k].tmp6.get(), 6, 6, r, -1.0, 1.0));
+            copy_group(cj, cx.st);
+            cj.clear();
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                mj.push_back(mv64(M.S6i.get(), 6, 6, 6, W[k].tmp6.get(), 6, r, W[k].dsw.get() + M.ns, M.nc, 1.0, 0.0));
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                mj.push_back(mv64(M.Z64.get(), M.ns, M.ns, 6, W[k].dsw.get() + M.ns, M.nc, r, W[k].dsw.get(), M.nc,
+                                  -1.0, 1.0));
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+        }
+        // (f) dt = y_t - Y [ds; dw]   (g) x += d
+        if (bounded) {
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                cj.push_back(cp64(W[k].yt64.get(), M.nt, W[k].dt.get(), M.nt, M.nt, r));
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const int ntp = sw[k]->tube->mt.lu.n;
+                mj.push_back(mv32(M.Y.get(), ntp, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+        }
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            const long long ldx = M.nt + M.nc;
+            if (bounded) cj.push_back(cp64(W[k].dt.get(), M.nt, xs[k], ldx, M.nt, r, 1.0, 1.0));
+            cj.push_back(cp64(W[k].dsw.get(), M.nc, xs[k] + M.nt, ldx, prescribed ? M.ns : M.nc, r, 1.0, 1.0));
+        }
+        copy_group(cj, cx.st);
+        cj.clear();
+        // (h) new residual
+        compute_residual();
+        const std::vector<double> rn = norms();
+        worst = 0;
+        for (size_t k = 0; k < G * r; ++k) {
+            const double rel = r0[k] > 0 ? std::sqrt(rn[k] / r0[k]) : 0.0;
+            worst = std::max(worst, rel);
+        }
+        if (!(worst == worst)) fail(SQBEM_ERR_NOT_CONVERGED, "mixed refinement produced a non-finite residual");
+    }
+    if (read_int(cx.err, cx.st)) fail(SQBEM_ERR_TIMEOUT, "mixed solve: a bounded wait in the tensor-core GEMM expired");
+    *iterations = it - 1;
+    *residual = worst;
+    if (worst > REFINE_TOL)
+        fail(SQBEM_ERR_NOT_CONVERGED, "mixed refinement reached relative residual %.3e after %d iterations", worst,
+             REFINE_MAX_IT);
+}
+
+}  // namespace sqbem

@@ -1,0 +1,72 @@
+// mixed_solver.cuh -- state of the SQBEM_MIXED swimmer path.
+//
+// Full system (t = tube, s = sphere, w = (U, Omega)), as in swimmer.hpp:11-16:
+//   [ T  B  Ct ] [f_t]   [b_t]        b_t = -A_uBt u_s
+//   [ D  E  Cs ] [f_s] = [b_s]        b_s = -A_uBs u_s
+//   [ 0  F  0  ] [ w ]   [ 0 ]        F: force-free / torque-free rows
+// Blocks are assembled in FP32 and kept for the FP64 residual.  The
+// preconditioner is the Schur elimination on split-BF16 tensor cores:
+// LU(T), Y = T^{-1}[B | Ct], G = [E | Cs] - D Y, LU(G_s), Z = G_s^{-1} G_c and
+// the 6 x 6 rigid-body system S6 = F Z solved in FP64.  Iterative refinement on
+// the full system, residuals accumulated in FP64, stops when the relative
+// residual reaches REFINE_TOL.
+#pragma once
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "mixed.cuh"
+
+namespace sqbem {
+
+constexpr double REFINE_TOL = 1e-11;
+constexpr int REFINE_MAX_IT = 30;
+
+struct MixedTube {
+    int nt = 0;
+    DevBuf<float> T;  // deflated T (nt x nt, column-major, ld nt), FP32
+    MixedLU lu;       // its factor (padded to a multiple of 128)
+};
+
+struct MixedSwimmer {
+    int ns = 0, nt = 0, nc = 0;       // 3 Ns, 3 Nt, 3 Ns + 6
+    DevBuf<float> B, AuBt;            // nt x ns
+    DevBuf<float> D;                  // ns x nt
+    DevBuf<float> E, AuBs;            // ns x ns
+    DevBuf<float> Ct, Cs;             // nt x 6, ns x 6
+    DevBuf<float> Y;                  // T^{-1} [B | Ct], ntp x nc (ld ntp)
+    DevBuf<bf16> Yh, Yl;              // its split column-major copy
+    DevBuf<bf16> Dh, Dl;              // D, split row-major (ld ntp, zero padding)
+    MixedLU G;                        // LU of G_s (padded)
+    DevBuf<float> Gc;                 // G_c, ns x 6
+    DevBuf<float> Z;                  // G_s^{-1} G_c, nsp x 6 (FP32)
+    DevBuf<bf16> Zh, Zl;
+    DevBuf<double> Z64;               // Z in FP64 (ns x 6)
+    DevBuf<double> F;                 // 6 x ns, column-major (ld 6), unscaled
+    DevBuf<double> S6i;               // (F Z)^{-1}, 6 x 6 column-major
+    DevBuf<double> K;                 // rigid-body map, ns x 6
+};
+
+}  // namespace sqbem
+
+struct sqbem_tube;
+struct sqbem_swimmer;
+
+namespace sqbem {
+struct MixedCtx;
+// Build the mixed tubes / swimmers of a group (equal padded tube size; for the
+// swimmers also equal sphere size).  The assembly runs per member, the dense
+// steps as grouped launches.
+void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx);
+void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx);
+// Refined solve of every member for nrhs right-hand sides; x = [f_t; f_s; w]
+// per member (device, FP64, (nt + nc) x nrhs), plus the iterations used and the
+// final relative residual (max over members and right-hand sides).
+//   prescribed = false: force- and torque-free swimming, in = slip fields
+//                       (device, ns x nrhs FP64), swimmer.hpp:107-139;
+//   prescribed = true:  rigid motion given, in = (U, Omega) (device, 6 x nrhs),
+//                       no slip and no constraint rows, swimmer.hpp:142-153.
+void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const std::vector<const double*>& in,
+                 int nrhs, const std::vector<double*>& x, const MixedCtx& cx, int* iterations, double* residual);
+}  // namespace sqbem

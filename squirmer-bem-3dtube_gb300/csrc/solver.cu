@@ -78,7 +78,14 @@ void sqbem_tube::build_device() {
     host_panels = make_panels(V.data(), Nt);
     panels.set(host_panels, st);
     const int n = 3 * Nt;
-    if (precision == SQBEM_MIXED) fail(SQBEM_ERR_ARG, "mixed precision tube: not available in this build");
+    if (precision == SQBEM_MIXED) {
+        DevBuf<int> flags(2, st);
+        flags.zero();
+        MixedCtx cx{st, flags.get(), flags.get() + 1};
+        mixed_build_tubes({this}, cx);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        return;
+    }
     DevBuf<double> T((size_t)n * n, st);
     auto job = block_job<double>(panels, panels, true, mu, T.get(), n, nullptr, 0);
     assemble_block(job, near_capacity(Nt, Nt), st, false);
@@ -97,7 +104,22 @@ void sqbem_swimmer::build(const sqbem_tube* t, int Ns_, const double* V, const d
     std::memcpy(xc, center, 3 * sizeof(double));
     host_panels = make_panels(V, Ns);
     panels.set(host_panels, st);
-    if (precision == SQBEM_MIXED) fail(SQBEM_ERR_ARG, "mixed precision swimmer: not available in this build");
+    if (precision == SQBEM_MIXED) {
+        if (tube && tube->precision != SQBEM_MIXED)
+            fail(SQBEM_ERR_ARG, "SwimmerSolver: a mixed-precision swimmer needs a mixed-precision tube");
+        EventTimer clock;
+        clock.start(st);
+        DevBuf<int> flags(2, st);
+        flags.zero();
+        MixedCtx cx{st, flags.get(), flags.get() + 1};
+        mixed_build_swimmers({this}, cx);
+        clock.stop(st);
+        t_assembly = 0;
+        t_schur = clock.seconds();
+        return;
+    }
+    if (tube && tube->precision != SQBEM_FP64)
+        fail(SQBEM_ERR_ARG, "SwimmerSolver: an FP64 swimmer needs an FP64 tube");
     build_fp64();
 }
 
@@ -154,6 +176,10 @@ void sqbem_swimmer::build_fp64() {
 void sqbem_swimmer::solve_free(int nrhs, const double* slips, double* U, double* Om, double* f_sphere,
                                double* f_tube) {
     const int ns = 3 * Ns, nt = 3 * Nt, n = ns + 6;
+    if (precision == SQBEM_MIXED) {
+        solve_mixed(false, nrhs, slips, U, Om, f_sphere, f_tube);
+        return;
+    }
     if (!haveM) {
         // M = [Gs | Gc ; scaled force/torque rows | 0]   (swimmer.hpp:108-125)
         DevBuf<double> M((size_t)n * n, st);
@@ -208,6 +234,12 @@ void sqbem_swimmer::solve_free(int nrhs, const double* slips, double* U, double*
 
 void sqbem_swimmer::solve_prescribed(const double* U, const double* Om, double* f_sphere, double* f_tube) {
     const int ns = 3 * Ns, nt = 3 * Nt, n = ns + 6;
+    if (precision == SQBEM_MIXED) {
+        const double w[6] = {U[0], U[1], U[2], Om[0], Om[1], Om[2]};
+        double Uo[3], Oo[3];
+        solve_mixed(true, 1, w, Uo, Oo, f_sphere, f_tube);
+        return;
+    }
     if (!haveGs) {
         luGs.factor(Gs.get(), ns, ns, st, "dgesv failed");
         haveGs = true;
@@ -299,4 +331,30 @@ void sqbem_duct::solve(double p_in, double p_out, double* u, double* f, double* 
     *Q = q;
     if (u) std::memcpy(u, uu.data(), sizeof(double) * n);
     if (f) std::memcpy(f, ff.data(), sizeof(double) * n);
+}
+
+// Mixed-precision solve for this swimmer alone (a group of one): in = slip
+// fields (Ns x 3 per right-hand side) or, if prescribed, (U, Omega) (6 values).
+void sqbem_swimmer::solve_mixed(bool prescribed, int nrhs, const double* in, double* U, double* Om, double* f_sphere,
+                                double* f_tube) {
+    const int ns = 3 * Ns, nt = 3 * Nt, nc = ns + 6;
+    const size_t per_in = prescribed ? 6 : (size_t)ns;
+    DevBuf<double> din(per_in * nrhs, st), x((size_t)(nt + nc) * nrhs, st);
+    din.upload(in, per_in * nrhs);
+    DevBuf<int> flags(2, st);
+    flags.zero();
+    MixedCtx cx{st, flags.get(), flags.get() + 1};
+    mixed_solve({this}, prescribed, {din.get()}, nrhs, {x.get()}, cx, &ir_iterations, &ir_residual);
+    std::vector<double> h((size_t)(nt + nc) * nrhs);
+    x.download(h.data(), h.size());
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    for (int k = 0; k < nrhs; ++k) {
+        const double* xk = h.data() + (size_t)k * (nt + nc);
+        for (int c = 0; c < 3; ++c) {
+            U[3 * k + c] = xk[nt + ns + c];
+            Om[3 * k + c] = xk[nt + ns + 3 + c];
+        }
+        if (f_sphere) std::memcpy(f_sphere + (size_t)k * ns, xk + nt, sizeof(double) * ns);
+        if (f_tube && nt) std::memcpy(f_tube + (size_t)k * nt, xk, sizeof(double) * nt);
+    }
 }

@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "dense.cuh"
 #include "mixed.cuh"
+#include "mixed_solver.cuh"
 
 namespace sqbem {
 
@@ -76,7 +77,7 @@ struct sqbem_tube {
     std::vector<sqbem::PanelRec> host_panels;
     sqbem::DevPanels panels;
     sqbem::LU64 lu;           // FP64 factor of the deflated T
-    sqbem::MixedLU mlu;       // mixed: split-BF16 factor of T (FP32 entries kept for residuals)
+    sqbem::MixedTube mt;      // mixed: FP32 T (for residuals) and its split-BF16 factor
     void build(double R, double L, double a, int n_theta, int n_r, double mu, int precision);
     void build_device();  // from `mesh` and the parameters already set
 };
@@ -108,6 +109,8 @@ struct sqbem_swimmer {
     void build_fp64();
     void solve_free(int nrhs, const double* slips, double* U, double* Om, double* f_sphere, double* f_tube);
     void solve_prescribed(const double* U, const double* Om, double* f_sphere, double* f_tube);
+    void solve_mixed(bool prescribed, int nrhs, const double* in, double* U, double* Om, double* f_sphere,
+                     double* f_tube);
 };
 
 // DuctFlow, src/duct_flow.hpp:22-109

@@ -93,8 +93,8 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
-__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((unsigned long long)map) : "memory");
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)map) : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
@@ -139,13 +139,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Problems of one launch travel as a __grid_constant__ kernel parameter (TMA
+// reads the tensor maps straight from parameter space; no device copies, so a
+// launch can be captured into a CUDA graph).
+constexpr int MAXP = 24;
 struct KArgs {
-    const TcProblem* probs;
-    const CUtensorMap* maps;  // 4 per problem: A_hi, A_lo, B_hi, B_lo
     int nprob;
     int total_tiles;
     int* err;
     int* flag;
+    TcProblem probs[MAXP];
+    CUtensorMap maps[4 * MAXP];  // A_hi, A_lo, B_hi, B_lo per problem
 };
 
 __device__ __forceinline__ int find_problem(const TcProblem* probs, int nprob, int t) {
@@ -158,7 +162,7 @@ __device__ __forceinline__ int find_problem(const TcProblem* probs, int nprob, i
     return lo;
 }
 
-__global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(KArgs args) {
+__global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_constant__ KArgs args) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -198,12 +202,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(KArgs args) {
         uint32_t ph = 0;
         int armed[STAGES] = {};
         int last_p = -1;
+        (void)last_p;
         for (int t = blockIdx.x; t < args.total_tiles; t += gridDim.x) {
             const int p = find_problem(args.probs, args.nprob, t);
             const TcProblem& P = args.probs[p];
-            const CUtensorMap* m = args.maps + 4 * p;
+            const CUtensorMap* m = &args.maps[4 * p];
             if (p != last_p) {
-                for (int j = 0; j < 4; ++j) tensormap_acquire(m + j);
+                for (int j = 0; j < 4; ++j) prefetch_tensormap(m + j);
                 last_p = p;
             }
             const int local = t - P.tile_start;
@@ -392,9 +397,22 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
              cudaStream_t st) {
     if (probs_in.size() != ops.size()) fail(SQBEM_ERR_ARG, "tc_gemm: operand count");
     get_encode();
-    std::vector<TcProblem> probs;
-    std::vector<CUtensorMap> maps;
-    int total = 0;
+    if (!g_num_sms) {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+        CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    }
+    KArgs a;
+    auto flush = [&](double flops, double bytes) {
+        if (a.nprob == 0) return;
+        const int grid = std::min(a.total_tiles, g_num_sms);
+        TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
+    };
+    a.nprob = 0;
+    a.total_tiles = 0;
+    a.err = err;
+    a.flag = flag;
     double flops = 0, bytes = 0;
     for (size_t i = 0; i < probs_in.size(); ++i) {
         TcProblem P = probs_in[i];
@@ -403,38 +421,25 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
         if (P.K <= 0) fail(SQBEM_ERR_ARG, "tc_gemm: K must be positive");
         if (o.A.rows < P.M || o.A.k < P.K || o.B.rows < P.N || o.B.k < P.K)
             fail(SQBEM_ERR_ARG, "tc_gemm: operand smaller than the problem");
+        if (a.nprob == MAXP) {
+            flush(flops, bytes);
+            a.nprob = 0;
+            a.total_tiles = 0;
+            flops = bytes = 0;
+        }
         P.tiles_n = ceil_div(P.N, BN);
-        P.tile_start = total;
-        total += ceil_div(P.M, BM) * P.tiles_n;
-        probs.push_back(P);
+        P.tile_start = a.total_tiles;
+        a.total_tiles += ceil_div(P.M, BM) * P.tiles_n;
         // maps cover exactly the problem's extent: rows beyond M / N and k beyond K read as zero
-        maps.push_back(make_map(o.A.hi, P.M, P.K, o.A.ld));
-        maps.push_back(make_map(o.A.lo, P.M, P.K, o.A.ld));
-        maps.push_back(make_map(o.B.hi, P.N, P.K, o.B.ld));
-        maps.push_back(make_map(o.B.lo, P.N, P.K, o.B.ld));
+        a.maps[4 * a.nprob + 0] = make_map(o.A.hi, P.M, P.K, o.A.ld);
+        a.maps[4 * a.nprob + 1] = make_map(o.A.lo, P.M, P.K, o.A.ld);
+        a.maps[4 * a.nprob + 2] = make_map(o.B.hi, P.N, P.K, o.B.ld);
+        a.maps[4 * a.nprob + 3] = make_map(o.B.lo, P.N, P.K, o.B.ld);
+        a.probs[a.nprob++] = P;
         flops += 2.0 * P.M * P.N * P.K;
         bytes += 4.0 * ((double)P.M * P.K + (double)P.K * P.N) + 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
     }
-    if (total == 0) return;
-    if (!g_num_sms) {
-        int dev = 0;
-        CUDA_CHECK(cudaGetDevice(&dev));
-        CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-        CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    }
-    DevBuf<TcProblem> dprobs(probs.size(), st);
-    DevBuf<CUtensorMap> dmaps(maps.size(), st);
-    dprobs.upload(probs.data(), probs.size());
-    dmaps.upload(maps.data(), maps.size());
-    KArgs a;
-    a.probs = dprobs.get();
-    a.maps = dmaps.get();
-    a.nprob = (int)probs.size();
-    a.total_tiles = total;
-    a.err = err;
-    a.flag = flag;
-    const int grid = std::min(total, g_num_sms);
-    TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
+    flush(flops, bytes);
 }
 
 }  // namespace sqbem
