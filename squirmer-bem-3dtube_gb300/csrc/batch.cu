@@ -4,7 +4,9 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <vector>
 
 #include "bem/utils/mesh.hpp"
@@ -100,6 +102,133 @@ void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStr
     res[15] = s.ir_iterations;
 }
 
+// Mixed precision: instances with equal padded tube size and equal sphere size
+// form a group; each group (in chunks of GROUP_MAX) is assembled member by
+// member and then factored, Schur-reduced and refined with grouped launches.
+constexpr int GROUP_MAX = 16;
+
+void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
+               double* results) {
+    std::map<std::tuple<int, int, int>, std::vector<int>> groups;
+    for (int k = 0; k < n; ++k) {
+        const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
+        groups[{prep[k].bounded ? 1 : 0, ntp, prep[k].sphere.P()}].push_back(k);
+    }
+    DevBuf<int> flags(2, bs);
+    for (auto& kv : groups) {
+        const std::vector<int>& all = kv.second;
+        for (size_t c0 = 0; c0 < all.size(); c0 += GROUP_MAX) {
+            const std::vector<int> ids(all.begin() + c0, all.begin() + std::min(all.size(), c0 + GROUP_MAX));
+            const size_t G = ids.size();
+            flags.zero();
+            MixedCtx cx{bs, flags.get(), flags.get() + 1};
+            std::vector<std::unique_ptr<sqbem_tube>> tubes(G);
+            std::vector<std::unique_ptr<sqbem_swimmer>> sws(G);
+            std::vector<sqbem_tube*> tp;
+            std::vector<sqbem_swimmer*> sp;
+            for (size_t g = 0; g < G; ++g) {
+                const Prepared& P = prep[ids[g]];
+                const sqbem_instance& in = inst[ids[g]];
+                if (P.bounded) {
+                    tubes[g] = std::make_unique<sqbem_tube>();
+                    sqbem_tube& t = *tubes[g];
+                    t.st.borrow(bs);
+                    t.R = P.R; t.L = P.L; t.a = 1.0; t.n_theta = in.n_theta; t.n_r = in.n_r; t.mu = 1.0;
+                    t.precision = SQBEM_MIXED;
+                    t.mesh = P.tube;
+                    t.set_panels();
+                    tp.push_back(&t);
+                }
+            }
+            if (!tp.empty()) mixed_build_tubes(tp, cx);
+            for (size_t g = 0; g < G; ++g) {
+                const Prepared& P = prep[ids[g]];
+                sws[g] = std::make_unique<sqbem_swimmer>();
+                sws[g]->st.borrow(bs);
+                const double c[3] = {P.b, 0, 0};
+                sws[g]->set_geometry(tubes[g].get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_MIXED);
+                sp.push_back(sws[g].get());
+            }
+            mixed_build_swimmers(sp, cx);
+            // the B1 = 1 and B2 = 1 slip modes of every member
+            std::vector<DevBuf<double>> slip(G), xs(G);
+            std::vector<const double*> in_ptr;
+            std::vector<double*> x_ptr;
+            for (size_t g = 0; g < G; ++g) {
+                sqbem_swimmer& s = *sws[g];
+                const double c[3] = {prep[ids[g]].b, 0, 0};
+                auto u1 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 1, 0);
+                const auto u2 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 0, 1);
+                u1.insert(u1.end(), u2.begin(), u2.end());
+                slip[g].alloc(u1.size(), bs);
+                slip[g].upload(u1.data(), u1.size());
+                xs[g].alloc((size_t)(s.mx.nt + s.mx.nc) * 2, bs);
+                in_ptr.push_back(slip[g].get());
+                x_ptr.push_back(xs[g].get());
+            }
+            int iters = 0;
+            double resid = 0;
+            mixed_solve(sp, false, in_ptr, 2, x_ptr, cx, &iters, &resid);
+            std::vector<std::vector<double>> hx(G);
+            for (size_t g = 0; g < G; ++g) {
+                hx[g].resize((size_t)(sws[g]->mx.nt + sws[g]->mx.nc) * 2);
+                xs[g].download(hx[g].data(), hx[g].size());
+            }
+            // towed drag of the members on the axis (main.cpp:90-91)
+            std::vector<sqbem_swimmer*> towed;
+            std::vector<size_t> towed_g;
+            for (size_t g = 0; g < G; ++g)
+                if (inst[ids[g]].towed && std::fabs(prep[ids[g]].b) < 1e-12) {
+                    towed.push_back(sws[g].get());
+                    towed_g.push_back(g);
+                }
+            std::vector<std::vector<double>> hf(towed.size());
+            if (!towed.empty()) {
+                const double w6[6] = {0, 0, 1, 0, 0, 0};
+                DevBuf<double> dw(6, bs);
+                dw.upload(w6, 6);
+                std::vector<DevBuf<double>> xt(towed.size());
+                std::vector<const double*> wi;
+                std::vector<double*> xo;
+                for (size_t t = 0; t < towed.size(); ++t) {
+                    xt[t].alloc((size_t)(towed[t]->mx.nt + towed[t]->mx.nc), bs);
+                    wi.push_back(dw.get());
+                    xo.push_back(xt[t].get());
+                }
+                int it2 = 0;
+                double r2 = 0;
+                mixed_solve(towed, true, wi, 1, xo, cx, &it2, &r2);
+                for (size_t t = 0; t < towed.size(); ++t) {
+                    hf[t].resize(xt[t].n);
+                    xt[t].download(hf[t].data(), hf[t].size());
+                }
+            }
+            CUDA_CHECK(cudaStreamSynchronize(bs));
+            for (size_t g = 0; g < G; ++g) {
+                sqbem_swimmer& s = *sws[g];
+                const int nt = s.mx.nt, ns = s.mx.ns, ldx = nt + s.mx.nc;
+                double* res = results + (size_t)ids[g] * SQBEM_RESULT_STRIDE;
+                for (int c = 0; c < 3; ++c) {
+                    res[c] = hx[g][nt + ns + c];
+                    res[3 + c] = hx[g][nt + ns + 3 + c];
+                    res[6 + c] = hx[g][ldx + nt + ns + c];
+                    res[9 + c] = hx[g][ldx + nt + ns + 3 + c];
+                }
+                res[12] = NAN;
+                res[13] = s.Nt;
+                res[14] = s.Ns;
+                res[15] = iters;
+            }
+            for (size_t t = 0; t < towed.size(); ++t) {
+                sqbem_swimmer& s = *towed[t];
+                double Fz = 0;
+                for (int p = 0; p < s.Ns; ++p) Fz = Fz - s.host_panels[p].area * hf[t][s.mx.nt + 3 * p + 2];
+                results[(size_t)ids[towed_g[t]] * SQBEM_RESULT_STRIDE + 12] = -Fz / (6 * bem::PI);
+            }
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
@@ -117,7 +246,10 @@ extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int pre
         Stream bs;
         EventTimer clk;
         clk.start(bs);
-        for (int k = 0; k < n; ++k) run_one(inst[k], prep[k], precision, bs, results + (size_t)k * SQBEM_RESULT_STRIDE);
+        if (precision == SQBEM_MIXED) run_mixed(n, inst, prep, bs, results);
+        else
+            for (int k = 0; k < n; ++k)
+                run_one(inst[k], prep[k], precision, bs, results + (size_t)k * SQBEM_RESULT_STRIDE);
         clk.stop(bs);
         const double secs = clk.seconds();
         if (device_seconds) *device_seconds = secs;

@@ -72,11 +72,15 @@ void sqbem_tube::build(double R_, double L_, double a_, int nth, int nr, double 
     build_device();
 }
 
-void sqbem_tube::build_device() {
+void sqbem_tube::set_panels() {
     Nt = mesh.P();
     const auto V = mesh_vertices(mesh);
     host_panels = make_panels(V.data(), Nt);
     panels.set(host_panels, st);
+}
+
+void sqbem_tube::build_device() {
+    set_panels();
     const int n = 3 * Nt;
     if (precision == SQBEM_MIXED) {
         DevBuf<int> flags(2, st);
@@ -95,7 +99,8 @@ void sqbem_tube::build_device() {
 }
 
 // ---------------------------------------------------------------- SwimmerSolver
-void sqbem_swimmer::build(const sqbem_tube* t, int Ns_, const double* V, const double* center, double mu_, int prec) {
+void sqbem_swimmer::set_geometry(const sqbem_tube* t, int Ns_, const double* V, const double* center, double mu_,
+                                 int prec) {
     tube = t;
     Ns = Ns_;
     Nt = t ? t->Nt : 0;
@@ -104,6 +109,10 @@ void sqbem_swimmer::build(const sqbem_tube* t, int Ns_, const double* V, const d
     std::memcpy(xc, center, 3 * sizeof(double));
     host_panels = make_panels(V, Ns);
     panels.set(host_panels, st);
+}
+
+void sqbem_swimmer::build(const sqbem_tube* t, int Ns_, const double* V, const double* center, double mu_, int prec) {
+    set_geometry(t, Ns_, V, center, mu_, prec);
     if (precision == SQBEM_MIXED) {
         if (tube && tube->precision != SQBEM_MIXED)
             fail(SQBEM_ERR_ARG, "SwimmerSolver: a mixed-precision swimmer needs a mixed-precision tube");

@@ -80,6 +80,7 @@ struct sqbem_tube {
     sqbem::MixedTube mt;      // mixed: FP32 T (for residuals) and its split-BF16 factor
     void build(double R, double L, double a, int n_theta, int n_r, double mu, int precision);
     void build_device();  // from `mesh` and the parameters already set
+    void set_panels();    // panel records only (the grouped mixed build factors later)
 };
 
 // host slip field (kernels.hpp:107-111) at the panel centroids, packed xyz
@@ -106,6 +107,8 @@ struct sqbem_swimmer {
     int ir_iterations = 0;
     double ir_residual = 0;
     void build(const sqbem_tube* tube, int Ns, const double* V, const double* center, double mu, int precision);
+    void set_geometry(const sqbem_tube* tube, int Ns, const double* V, const double* center, double mu,
+                      int precision);
     void build_fp64();
     void solve_free(int nrhs, const double* slips, double* U, double* Om, double* f_sphere, double* f_tube);
     void solve_prescribed(const double* U, const double* Om, double* f_sphere, double* f_tube);

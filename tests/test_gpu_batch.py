@@ -1,0 +1,64 @@
+"""Batched kinematics (sqbem_kinematics_batch): the grouped mixed-precision
+batch against the FP64 batch and against the reference fixtures."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+sqbem = pytest.importorskip("sqbem")
+from sqbem import workloads  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def uo_err(a, b):
+    """norm-wise relative error of (U_B1, Om_B1, U_B2, Om_B2) per instance"""
+    return np.linalg.norm(a[:, :12] - b[:, :12], axis=1) / np.linalg.norm(b[:, :12], axis=1)
+
+
+def test_batch_small_mixed_vs_fp64():
+    rng = np.random.default_rng(5)
+    insts = []
+    for k in range(10):
+        lam = rng.uniform(0.15, 0.55)
+        e = rng.normal(size=3)
+        e /= np.linalg.norm(e)
+        insts.append(dict(a_over_R=lam, beta=rng.uniform(0, 0.8 * (1 - lam)), L_over_R=4.0, e=tuple(e),
+                          n_theta=int(rng.choice([8, 12])), n_r=4, sphere_level=int(rng.choice([1, 2])),
+                          towed=1))
+    insts.append(dict(a_over_R=0.0, beta=0.0, L_over_R=4.0, e=(0, 0, 1.0), n_theta=0, n_r=4, sphere_level=2, towed=1))
+    insts.append(dict(a_over_R=0.3, beta=0.0, L_over_R=4.0, e=(0, 0, 1.0), n_theta=12, n_r=4, sphere_level=1, towed=1))
+    r64, t64 = sqbem.kinematics_batch(insts, sqbem.FP64)
+    rmx, tmx = sqbem.kinematics_batch(insts, sqbem.MIXED)
+    assert t64 > 0 and tmx > 0
+    np.testing.assert_array_equal(r64[:, 13:15], rmx[:, 13:15])  # Nt, Ns
+    assert np.all(uo_err(rmx, r64) < 1e-6), uo_err(rmx, r64)
+    towed = ~np.isnan(r64[:, 12])
+    assert towed.sum() == 2
+    np.testing.assert_allclose(rmx[towed, 12], r64[towed, 12], rtol=1e-6)
+    assert np.all(rmx[:, 15] >= 1)
+
+
+def test_batch_fp64_matches_single_solves():
+    g = golden("c2_l2")["l2_off"]
+    inst = dict(a_over_R=g["a_over_R"], beta=g["beta"], L_over_R=4.0, e=tuple(g["e"]), n_theta=24, n_r=4,
+                sphere_level=2, towed=0)
+    r, _ = sqbem.kinematics_batch([inst], sqbem.FP64)
+    ref = np.concatenate([g["B1"]["U"], g["B1"]["Om"], g["B2"]["U"], g["B2"]["Om"]])
+    assert np.max(np.abs(r[0, :12] - ref)) < 1e-10 * np.max(np.abs(ref))
+
+
+def test_batch_sweep_instances_mixed_vs_fp64():
+    """the first instances of the seeded sweep workload (n_theta = 24, levels 2 and 3)"""
+    insts = workloads.sweep()[:6]
+    r64, _ = sqbem.kinematics_batch(insts, sqbem.FP64)
+    rmx, _ = sqbem.kinematics_batch(insts, sqbem.MIXED)
+    err = uo_err(rmx, r64)
+    assert np.all(err < 1e-6), err
+
+
+def test_batch_rejects_bad_instances():
+    with pytest.raises(sqbem.BEMError):
+        sqbem.kinematics_batch([dict(a_over_R=1.5, beta=0.0, sphere_level=2)], sqbem.MIXED)
+    with pytest.raises(sqbem.BEMError):
+        sqbem.kinematics_batch([dict(a_over_R=0.3, beta=0.0, sphere_level=2, e=(0, 0, 2.0))], sqbem.MIXED)
