@@ -217,9 +217,21 @@ __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y,
 constexpr int FAR_TGT = 64;   // targets per CTA (threads)
 constexpr int FAR_SRC = 16;   // source panels per CTA
 
+// FP32 view of a source panel for the mixed far field: vertex offsets from the
+// centroid (exact in FP64, rounded once), normal, area, and the FP64 squared
+// far-field radius (3 h)^2 of the rule test.
+struct FarF {
+    float d[9];
+    float n[3];
+    float area;
+    float pad;
+    double far2;
+};
+
 template <class TO, class TC>
 __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
     __shared__ PanelRec sp[FAR_SRC];
+    __shared__ FarF sf[FAR_SRC];
     const int p0 = blockIdx.y * FAR_SRC;
     const int ns = min(FAR_SRC, job.nS - p0);
     {
@@ -229,46 +241,75 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
         for (int k = threadIdx.x; k < nd; k += blockDim.x) dst[k] = src[k];
     }
     __syncthreads();
+    if constexpr (sizeof(TC) == 4) {
+        if (threadIdx.x < ns) {
+            const PanelRec& P = sp[threadIdx.x];
+            FarF& F = sf[threadIdx.x];
+            for (int k = 0; k < 9; ++k) F.d[k] = (float)(P.v[k] - P.c[k % 3]);
+            F.n[0] = (float)P.n[0]; F.n[1] = (float)P.n[1]; F.n[2] = (float)P.n[2];
+            F.area = (float)P.area;
+            F.far2 = 9.0 * P.h * P.h;
+        }
+        __syncthreads();
+    }
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     if (i >= job.nT) return;
     const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
+    const TC ss = (TC)job.sscale, ds = (TC)job.dscale;
     for (int s = 0; s < ns; ++s) {
         const PanelRec& P = sp[s];
         const int p = p0 + s;
         const bool self = job.same_mesh && p == i;
-        const int rule = self ? 4 : rule_of(P, x, y, z);
-        if (rule != 0) {
-            const int slot = atomicAdd(job.near_count, 1);
-            if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
-            continue;
-        }
         Acc<TC> A;
         A.zero();
-        const TC e0x = (TC)(P.v[0] - x), e0y = (TC)(P.v[1] - y), e0z = (TC)(P.v[2] - z);
-        const TC e1x = (TC)(P.v[3] - x), e1y = (TC)(P.v[4] - y), e1z = (TC)(P.v[5] - z);
-        const TC e2x = (TC)(P.v[6] - x), e2y = (TC)(P.v[7] - y), e2z = (TC)(P.v[8] - z);
-        const TC mx = (TC)P.n[0], my = (TC)P.n[1], mz = (TC)P.n[2];
-        const TC area = (TC)P.area;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) {
-            TC l0, l1, l2, w;
-            if constexpr (sizeof(TC) == 8) {
-                l0 = c_rule7[q].l0; l1 = c_rule7[q].l1; l2 = c_rule7[q].l2; w = c_rule7[q].w;
-            } else {
-                l0 = c_rule7f[q].l0; l1 = c_rule7f[q].l1; l2 = c_rule7f[q].l2; w = c_rule7f[q].w;
+        if constexpr (sizeof(TC) == 8) {
+            const int rule = self ? 4 : rule_of(P, x, y, z);
+            if (rule != 0) {
+                const int slot = atomicAdd(job.near_count, 1);
+                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
+                continue;
             }
-            const TC rx = l0 * e0x + l1 * e1x + l2 * e2x;
-            const TC ry = l0 * e0y + l1 * e1y + l2 * e2y;
-            const TC rz = l0 * e0z + l1 * e1z + l2 * e2z;
-            accum<TC, true>(A, rx, ry, rz, w * area, mx, my, mz);
+            const double e0x = P.v[0] - x, e0y = P.v[1] - y, e0z = P.v[2] - z;
+            const double e1x = P.v[3] - x, e1y = P.v[4] - y, e1z = P.v[5] - z;
+            const double e2x = P.v[6] - x, e2y = P.v[7] - y, e2z = P.v[8] - z;
+            const double mx = P.n[0], my = P.n[1], mz = P.n[2], area = P.area;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                const double l0 = c_rule7[q].l0, l1 = c_rule7[q].l1, l2 = c_rule7[q].l2, w = c_rule7[q].w;
+                accum<double, true>(A, l0 * e0x + l1 * e1x + l2 * e2x, l0 * e0y + l1 * e1y + l2 * e2y,
+                                    l0 * e0z + l1 * e1z + l2 * e2z, w * area, mx, my, mz);
+            }
+        } else {
+            // rule test on the squared distance in FP64; the reference's exact test
+            // (sqrt, division) only inside a +-1e-12 band around the threshold
+            const double cx = P.c[0] - x, cy = P.c[1] - y, cz = P.c[2] - z;
+            const double d2 = cx * cx + cy * cy + cz * cz;
+            const FarF& F = sf[s];
+            bool near = self || d2 < F.far2 * (1.0 - 1e-12);
+            if (!near && !(d2 > F.far2 * (1.0 + 1e-12))) near = rule_of(P, x, y, z) != 0;
+            if (near) {
+                const int slot = atomicAdd(job.near_count, 1);
+                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | ((self ? 4 : 1) << 28));
+                continue;
+            }
+            // r = (c - x0) + sum_k l_k (V_k - c): FP64 only in the centroid offset
+            const float bx = (float)cx, by = (float)cy, bz = (float)cz;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                const float l0 = c_rule7f[q].l0, l1 = c_rule7f[q].l1, l2 = c_rule7f[q].l2, w = c_rule7f[q].w;
+                const float rx = bx + (l0 * F.d[0] + l1 * F.d[3] + l2 * F.d[6]);
+                const float ry = by + (l0 * F.d[1] + l1 * F.d[4] + l2 * F.d[7]);
+                const float rz = bz + (l0 * F.d[2] + l1 * F.d[5] + l2 * F.d[8]);
+                accum<float, true>(A, rx, ry, rz, w * F.area, F.n[0], F.n[1], F.n[2]);
+            }
         }
 #pragma unroll
         for (int b = 0; b < 3; ++b)
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const long long r = 3LL * i + a, c = 3LL * p + b;
-                if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)((double)sl_entry(A, a, b) * job.sscale);
-                if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)((double)dl_entry(A, a, b) * job.dscale);
+                if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)(sl_entry(A, a, b) * ss);
+                if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)(dl_entry(A, a, b) * ds);
             }
     }
 }
@@ -282,9 +323,11 @@ __global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
     const int count = min(*job.near_count, job.near_cap);
     for (int k = warp; k < count; k += nwarps) {
         const int2 e = job.near_list[k];
-        const int i = e.x, p = e.y & 0x0fffffff, rule = e.y >> 28;
+        const int i = e.x, p = e.y & 0x0fffffff;
         const PanelRec P = job.src[p];
         const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
+        // the far kernel may only have marked the pair as near: the exact rule here
+        const int rule = (e.y >> 28) == 4 ? 4 : rule_of(P, x, y, z);
         double sl = 0, dl = 0;
         const int a = lane / 3, b = lane % 3;
         if (rule == 4) {
@@ -327,8 +370,8 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     if (mixed) TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
     else TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
     const int warps = 152 * 16;
-    if (mixed) LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
-    else LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
+    if (mixed) TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
+    else TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
     if ((long long)job.nT * job.nS > near_cap) {
         // the list could overflow only for blocks larger than its capacity
         int h = 0;

@@ -105,7 +105,7 @@ void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStr
 // Mixed precision: instances with equal padded tube size and equal sphere size
 // form a group; each group (in chunks of GROUP_MAX) is assembled member by
 // member and then factored, Schur-reduced and refined with grouped launches.
-constexpr int GROUP_MAX = 16;
+constexpr int GROUP_MAX = 48;
 
 void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
                double* results) {

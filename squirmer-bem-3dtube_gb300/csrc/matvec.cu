@@ -16,7 +16,7 @@ namespace sqbem {
 namespace {
 
 constexpr int MV_ROWS = 128;
-constexpr int MV_CHUNK = 64;
+constexpr int MV_CHUNK = 256;
 constexpr int MV_RMAX = 8;
 
 constexpr int MAXJOBS = 48;
@@ -24,6 +24,7 @@ struct MvDev {
     MvJob j;
     long long part_off;  // offset of this job's partials in the scratch
     int nchunk;
+    int rstride;         // partials per row (= r)
 };
 struct MvArgs {
     int n;
@@ -38,6 +39,7 @@ struct NormArgs {
     NormJob j[MAXJOBS];
 };
 
+template <int R>
 __global__ void __launch_bounds__(MV_ROWS) mv_partial(const __grid_constant__ MvArgs args, double* __restrict__ part) {
     const MvDev& D = args.j[blockIdx.z];
     const MvJob& J = D.j;
@@ -45,18 +47,33 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial(const __grid_constant__ Mv
     const int c = blockIdx.y;
     if (c >= D.nchunk || row >= J.m) return;
     const int j0 = c * MV_CHUNK, j1 = min(J.n, j0 + MV_CHUNK);
-    double s[MV_RMAX];
+    double s[R];
 #pragma unroll
-    for (int k = 0; k < MV_RMAX; ++k) s[k] = 0.0;
-    for (int j = j0; j < j1; ++j) {
-        const double a = J.A32 ? (double)J.A32[row + (long long)j * J.lda] : J.A64[row + (long long)j * J.lda];
+    for (int k = 0; k < R; ++k) s[k] = 0.0;
+    const int r = J.r;
+    if (J.A32) {
+        const float* a = J.A32 + row + (long long)j0 * J.lda;
+#pragma unroll 8
+        for (int j = j0; j < j1; ++j, a += J.lda) {
+            const double v = (double)__ldg(a);
 #pragma unroll
-        for (int k = 0; k < MV_RMAX; ++k)
-            if (k < J.r) s[k] = fma(a, J.x[j + (long long)k * J.ldx], s[k]);
+            for (int k = 0; k < R; ++k)
+                if (k < r) s[k] = fma(v, __ldg(J.x + j + (long long)k * J.ldx), s[k]);
+        }
+    } else {
+        const double* a = J.A64 + row + (long long)j0 * J.lda;
+#pragma unroll 4
+        for (int j = j0; j < j1; ++j, a += J.lda) {
+            const double v = __ldg(a);
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+                if (k < r) s[k] = fma(v, __ldg(J.x + j + (long long)k * J.ldx), s[k]);
+        }
     }
-    double* o = part + D.part_off + ((long long)c * J.m + row) * MV_RMAX;
+    double* o = part + D.part_off + ((long long)c * J.m + row) * D.rstride;
 #pragma unroll
-    for (int k = 0; k < MV_RMAX; ++k) o[k] = s[k];
+    for (int k = 0; k < R; ++k)
+        if (k < r) o[k] = s[k];
 }
 
 __global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __restrict__ part) {
@@ -66,7 +83,7 @@ __global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __r
     if (row >= J.m) return;
     for (int k = 0; k < J.r; ++k) {
         double s = 0.0;
-        for (int c = 0; c < D.nchunk; ++c) s += part[D.part_off + ((long long)c * J.m + row) * MV_RMAX + k];
+        for (int c = 0; c < D.nchunk; ++c) s += part[D.part_off + ((long long)c * J.m + row) * D.rstride + k];
         double* y = J.y + row + (long long)k * J.ldy;
         *y = J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * *y);
     }
@@ -122,21 +139,24 @@ void matvec_group(const std::vector<MvJob>& jobs_in, cudaStream_t st) {
         MvArgs a;
         a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
         long long off = 0;
-        int maxm = 0, maxc = 0;
+        int maxm = 0, maxc = 0, maxr = 0;
         double bytes = 0;
         for (int k = 0; k < a.n; ++k) {
             const MvJob& j = jobs[i0 + k];
             a.j[k].j = j;
             a.j[k].nchunk = std::max(1, ceil_div(j.n, MV_CHUNK));
             a.j[k].part_off = off;
-            off += (long long)a.j[k].nchunk * j.m * MV_RMAX;
+            a.j[k].rstride = j.r;
+            off += (long long)a.j[k].nchunk * j.m * j.r;
+            maxr = std::max(maxr, j.r);
             maxm = std::max(maxm, j.m);
             maxc = std::max(maxc, a.j[k].nchunk);
             bytes += (double)j.m * j.n * (j.A32 ? 4 : 8);
         }
         DevBuf<double> part((size_t)off, st);
-        TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial, dim3(ceil_div(maxm, MV_ROWS), maxc, (unsigned)a.n), MV_ROWS, 0,
-                     st, a, part.get());
+        const dim3 grid(ceil_div(maxm, MV_ROWS), maxc, (unsigned)a.n);
+        if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<2>, grid, MV_ROWS, 0, st, a, part.get());
+        else TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
         LAUNCH(mv_finish, dim3(ceil_div(maxm, 128), (unsigned)a.n), 128, 0, st, a, part.get());
     }
 }
@@ -153,8 +173,8 @@ void copy_group(const std::vector<CopyJob>& jobs_in, cudaStream_t st) {
             a.j[k] = jobs[i0 + k];
             mx = std::max(mx, (long long)a.j[k].rows * a.j[k].cols);
         }
-        LAUNCH(copy_kernel_g, dim3((unsigned)std::min<long long>(ceil_div(mx, 256), 2048), (unsigned)a.n), 256, 0, st,
-               a);
+        TIMED_LAUNCH("copy", 0.0, 0.0, copy_kernel_g,
+                     dim3((unsigned)std::min<long long>(ceil_div(mx, 256), 2048), (unsigned)a.n), 256, 0, st, a);
     }
 }
 

@@ -169,7 +169,7 @@ void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
         a.flag = cx.flag;
         const int n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
         for (int k = 0; k < n; ++k) a.j[k] = jobs[i0 + k];
-        LAUNCH(diag_kernel, n, DIAG_THREADS, DIAG_SMEM, cx.st, a);
+        TIMED_LAUNCH("lu_diag", 0.0, 0.0, diag_kernel, n, DIAG_THREADS, DIAG_SMEM, cx.st, a);
     }
 }
 
@@ -359,7 +359,7 @@ void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
         }
         if (mx == 0) continue;
         const int gx = (int)std::min<long long>(ceil_div(mx, 256), 2048);
-        LAUNCH(conv_kernel, dim3(gx, (unsigned)a.n), 256, 0, st, a);
+        TIMED_LAUNCH("convert", 0.0, 0.0, conv_kernel, dim3(gx, (unsigned)a.n), 256, 0, st, a);
     }
 }
 

@@ -1,9 +1,10 @@
 // mixed_solver.cu -- the SQBEM_MIXED swimmer path over groups of instances.
 //
 // Build (per group): FP32 assembly of every block (FP64 relative vectors, FP64
-// 448-point and self integrals), LU(T) and Y = T^{-1}[B | Ct] on the tensor
-// cores, G = [E | Cs] - D Y, LU(G_s), Z = G_s^{-1} G_c, S6 = F Z inverted in
-// FP64 on the host (6 x 6).
+// 448-point and self integrals); T^{-1} and G_s^{-1} by the certified LU and the
+// LU solve of the identity on the tensor cores; Y = T^{-1}[B | Ct] and
+// [G_s | G_c] = [E | Cs] - D Y as grouped tensor-core GEMMs; Z = G_s^{-1} G_c
+// and S6 = F Z in FP64, S6 inverted on the host (6 x 6).
 // Solve: iterative refinement of the full system in FP64 (see mixed_solver.cuh).
 #include <cuda_runtime.h>
 
@@ -134,43 +135,86 @@ MvJob mv64(const double* A, long long lda, int m, int n, const double* x, long l
 
 }  // namespace
 
+// ---------------------------------------------------------------- inverses
+// inv[k] (n x n, column-major, ld n) <- A_k^{-1} from the factor L[k], with an
+// optional row-major split copy (rh/rl).  Solves the identity in place.
+static void invert_group(const std::vector<MixedLU*>& L, const std::vector<float*>& inv,
+                         const std::vector<bf16*>& rh, const std::vector<bf16*>& rl, const MixedCtx& cx) {
+    const size_t G = L.size();
+    std::vector<DevBuf<bf16>> ch(G), cl(G);
+    std::vector<Rhs> rhs(G);
+    for (size_t k = 0; k < G; ++k) {
+        const int n = L[k]->n;
+        CUDA_CHECK(cudaMemsetAsync(inv[k], 0, sizeof(float) * (size_t)n * n, cx.st));
+        pad_identity(inv[k], n, 0, n, cx.st);
+        ch[k].alloc((size_t)n * n, cx.st);
+        cl[k].alloc((size_t)n * n, cx.st);
+        Rhs& r = rhs[k];
+        r.X = inv[k]; r.ldx = n; r.nrhs = n; r.Sh = ch[k].get(); r.Sl = cl[k].get(); r.lds = n;
+        r.Rh = rh.empty() ? nullptr : rh[k];
+        r.Rl = rl.empty() ? nullptr : rl[k];
+        r.ldr = n;
+    }
+    mixed_lu_solve(L, rhs, cx);
+}
+
 // ---------------------------------------------------------------- tubes
 void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx) {
+    const size_t G = tubes.size();
+    std::vector<MixedLU> lu(G);
     std::vector<MixedLU*> lus;
     std::vector<CopyJob> cj;
-    for (sqbem_tube* t : tubes) {
+    for (size_t k = 0; k < G; ++k) {
+        sqbem_tube* t = tubes[k];
         MixedTube& M = t->mt;
         M.nt = 3 * t->Nt;
-        M.lu.alloc(M.nt, cx.st);
-        const int np = M.lu.n;
-        M.lu.A.zero();
-        auto job = fjob(t->panels, t->panels, true, t->mu, M.lu.A.get(), np, nullptr, 0);
+        lu[k].alloc(M.nt, cx.st);
+        M.ntp = lu[k].n;
+        const int np = M.ntp;
+        lu[k].A.zero();
+        auto job = fjob(t->panels, t->panels, true, t->mu, lu[k].A.get(), np, nullptr, 0);
         assemble_block(job, cap_pairs(t->Nt, t->Nt), cx.st, true);
-        deflate<float>(M.lu.A.get(), 1, np, t->panels, t->mu, cx.st);
-        pad_identity(M.lu.A.get(), np, M.nt, np, cx.st);
+        deflate<float>(lu[k].A.get(), 1, np, t->panels, t->mu, cx.st);
+        pad_identity(lu[k].A.get(), np, M.nt, np, cx.st);
         M.T.alloc((size_t)M.nt * M.nt, cx.st);
-        cj.push_back(cp32_32(M.lu.A.get(), np, M.T.get(), M.nt, M.nt, M.nt));
-        lus.push_back(&M.lu);
+        cj.push_back(cp32_32(lu[k].A.get(), np, M.T.get(), M.nt, M.nt, M.nt));
+        lus.push_back(&lu[k]);
     }
     copy_group(cj, cx.st);
     mixed_lu_factor(lus, cx);
     check_ctx(cx, "dgetrf (mixed tube factor)");
+    std::vector<float*> inv;
+    std::vector<bf16*> rh, rl;
+    for (sqbem_tube* t : tubes) {
+        MixedTube& M = t->mt;
+        const size_t nn = (size_t)M.ntp * M.ntp;
+        M.Ti.alloc(nn, cx.st);
+        M.TiRh.alloc(nn, cx.st);
+        M.TiRl.alloc(nn, cx.st);
+        inv.push_back(M.Ti.get());
+        rh.push_back(M.TiRh.get());
+        rl.push_back(M.TiRl.get());
+    }
+    invert_group(lus, inv, rh, rl, cx);
+    check_ctx(cx, "mixed tube inverse");
 }
 
 // ---------------------------------------------------------------- swimmers
 void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx) {
     if (sw.empty()) return;
+    const size_t G = sw.size();
     const bool bounded = sw[0]->tube != nullptr;
     std::vector<CopyJob> cj;
     std::vector<MvJob> mj;
     std::vector<DevBuf<double>> tmp;
-    tmp.reserve(2 * sw.size());
+    tmp.reserve(2 * G);
     for (sqbem_swimmer* s : sw) {
         MixedSwimmer& M = s->mx;
         const int Ns = s->Ns, Nt = s->Nt;
         M.ns = 3 * Ns;
         M.nt = 3 * Nt;
         M.nc = M.ns + 6;
+        M.nsp = pad128(M.ns);
         const int ns = M.ns, nt = M.nt;
         M.E.alloc((size_t)ns * ns, cx.st);
         M.AuBs.alloc((size_t)ns * ns, cx.st);
@@ -192,7 +236,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         add_rowsums<float>(M.AuBs.get(), 1, ns, ns, Ns, rsum.get(), cx.st);
         diag_complete<float>(M.AuBs.get(), 1, ns, Ns, rsum.get(), bounded ? 0.0 : 1.0, nullptr, cx.st);
         deflate<float>(M.E.get(), 1, ns, s->panels, s->mu, cx.st);
-        // rigid-body map, C = A_u K (accumulated in FP64, stored FP32)
+        // rigid-body map, C = A_u K (accumulated in FP64, stored FP32)   (swimmer.hpp:222-234)
         const auto Kh = rigid_map(s->host_panels, s->xc);
         M.K.alloc(Kh.size(), cx.st);
         M.K.upload(Kh.data(), Kh.size());
@@ -216,121 +260,121 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
     mj.clear();
     tmp.clear();
 
-    // Schur complement: Y = T^{-1} [B | Ct];  [G_s | G_c] = [E | Cs] - D Y
-    if (bounded) {
-        std::vector<MixedLU*> tl;
-        std::vector<Rhs> rh;
-        for (sqbem_swimmer* s : sw) {
-            MixedSwimmer& M = s->mx;
-            MixedLU& L = const_cast<sqbem_tube*>(s->tube)->mt.lu;
-            const int ntp = L.n;
-            M.Y.alloc((size_t)ntp * M.nc, cx.st);
-            M.Y.zero();
-            M.Yh.alloc((size_t)ntp * M.nc, cx.st);
-            M.Yl.alloc((size_t)ntp * M.nc, cx.st);
-            cj.push_back(cp32_32(M.B.get(), M.nt, M.Y.get(), ntp, M.nt, M.ns));
-            cj.push_back(cp32_32(M.Ct.get(), M.nt, M.Y.get() + (size_t)ntp * M.ns, ntp, M.nt, 6));
-            tl.push_back(&L);
-            Rhs r;
-            r.X = M.Y.get(); r.ldx = ntp; r.nrhs = M.nc; r.Sh = M.Yh.get(); r.Sl = M.Yl.get(); r.lds = ntp;
-            rh.push_back(r);
-        }
-        copy_group(cj, cx.st);
-        cj.clear();
-        mixed_lu_solve(tl, rh, cx);
-    }
+    // G = [E | Cs] (- D Y with Y = T^{-1} [B | Ct] when bounded), G_s padded
+    std::vector<MixedLU> glu(G);
     std::vector<MixedLU*> gl;
-    std::vector<ConvJob> conv;
-    for (sqbem_swimmer* s : sw) {
-        MixedSwimmer& M = s->mx;
-        M.G.alloc(M.ns, cx.st);
-        const int nsp = M.G.n;
-        M.G.A.zero();
-        cj.push_back(cp32_32(M.E.get(), M.ns, M.G.A.get(), nsp, M.ns, M.ns));
-        pad_identity(M.G.A.get(), nsp, M.ns, nsp, cx.st);
-        M.Gc.alloc((size_t)M.ns * 6, cx.st);
-        cj.push_back(cp32_32(M.Cs.get(), M.ns, M.Gc.get(), M.ns, M.ns, 6));
-        if (bounded) {
-            const int ntp = s->tube->mt.lu.n;
-            M.Dh.alloc((size_t)M.ns * ntp, cx.st);
-            M.Dl.alloc((size_t)M.ns * ntp, cx.st);
-            M.Dh.zero();
-            M.Dl.zero();
-            conv.push_back({M.D.get(), 1, M.ns, M.ns, M.nt, M.Dh.get(), M.Dl.get(), ntp, 1});
-        }
-        gl.push_back(&M.G);
+    std::vector<DevBuf<float>> Gc(G);
+    for (size_t k = 0; k < G; ++k) {
+        MixedSwimmer& M = sw[k]->mx;
+        glu[k].alloc(M.ns, cx.st);
+        glu[k].A.zero();
+        cj.push_back(cp32_32(M.E.get(), M.ns, glu[k].A.get(), M.nsp, M.ns, M.ns));
+        pad_identity(glu[k].A.get(), M.nsp, M.ns, M.nsp, cx.st);
+        Gc[k].alloc((size_t)M.ns * 6, cx.st);
+        cj.push_back(cp32_32(M.Cs.get(), M.ns, Gc[k].get(), M.ns, M.ns, 6));
+        gl.push_back(&glu[k]);
     }
     copy_group(cj, cx.st);
     cj.clear();
     if (bounded) {
+        // [B | Ct] -> split (column-major, ld ntp, zero rows beyond nt); D -> split (row-major, ld ntp)
+        std::vector<DevBuf<bf16>> bch(G), bcl(G), yh(G), yl(G), dh(G), dl(G);
+        std::vector<ConvJob> conv;
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            const int ntp = sw[k]->tube->mt.ntp;
+            const size_t sz = (size_t)ntp * M.nc;
+            bch[k].alloc(sz, cx.st); bcl[k].alloc(sz, cx.st); bch[k].zero(); bcl[k].zero();
+            yh[k].alloc(sz, cx.st); yl[k].alloc(sz, cx.st); yh[k].zero(); yl[k].zero();
+            dh[k].alloc((size_t)M.ns * ntp, cx.st); dl[k].alloc((size_t)M.ns * ntp, cx.st);
+            dh[k].zero(); dl[k].zero();
+            conv.push_back({M.B.get(), 1, M.nt, M.nt, M.ns, bch[k].get(), bcl[k].get(), 1, ntp});
+            conv.push_back({M.Ct.get(), 1, M.nt, M.nt, 6, bch[k].get() + (size_t)ntp * M.ns,
+                            bcl[k].get() + (size_t)ntp * M.ns, 1, ntp});
+            conv.push_back({M.D.get(), 1, M.ns, M.ns, M.nt, dh[k].get(), dl[k].get(), ntp, 1});
+        }
         convert_group(conv, cx.st);
+        // Y = T^{-1} [B | Ct]   (FP32 for the refinement, split for the Schur product)
         std::vector<TcProblem> P;
         std::vector<TcOperands> O;
-        for (sqbem_swimmer* s : sw) {
-            MixedSwimmer& M = s->mx;
-            const int ntp = s->tube->mt.lu.n, nsp = M.G.n;
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            const MixedTube& Tt = sw[k]->tube->mt;
+            const int ntp = Tt.ntp;
+            M.Y.alloc((size_t)M.nt * M.nc, cx.st);
+            TcProblem p;
+            p.M = M.nt; p.N = M.nc; p.K = M.nt; p.alpha = 1.f; p.beta = 0.f;
+            p.C = M.Y.get(); p.c_rs = 1; p.c_cs = M.nt;
+            p.O_hi = yh[k].get(); p.O_lo = yl[k].get(); p.o_rs = 1; p.o_cs = ntp;
             TcOperands o;
-            o.A = {M.Dh.get(), M.Dl.get(), M.ns, ntp, ntp};
+            o.A = {const_cast<bf16*>(Tt.TiRh.get()), const_cast<bf16*>(Tt.TiRl.get()), M.nt, M.nt, ntp};
+            o.B = {bch[k].get(), bcl[k].get(), M.nc, M.nt, ntp};
+            P.push_back(p);
+            O.push_back(o);
+        }
+        tc_gemm(P, O, cx.err, nullptr, cx.st);
+        P.clear();
+        O.clear();
+        // [G_s | G_c] -= D Y
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            const int ntp = sw[k]->tube->mt.ntp;
+            TcOperands o;
+            o.A = {dh[k].get(), dl[k].get(), M.ns, ntp, ntp};
+            o.B = {yh[k].get(), yl[k].get(), M.ns, ntp, ntp};
             TcProblem p;
             p.M = M.ns; p.N = M.ns; p.K = ntp; p.alpha = -1.f; p.beta = 1.f;
-            p.C = M.G.A.get(); p.c_rs = 1; p.c_cs = nsp;
-            o.B = {M.Yh.get(), M.Yl.get(), M.ns, ntp, ntp};
+            p.C = glu[k].A.get(); p.c_rs = 1; p.c_cs = M.nsp;
             P.push_back(p);
             O.push_back(o);
             TcProblem q = p;
             q.N = 6;
-            q.C = M.Gc.get(); q.c_cs = M.ns;
+            q.C = Gc[k].get(); q.c_cs = M.ns;
             TcOperands o2 = o;
-            o2.B = {M.Yh.get() + (size_t)ntp * M.ns, M.Yl.get() + (size_t)ntp * M.ns, 6, ntp, ntp};
+            o2.B = {yh[k].get() + (size_t)ntp * M.ns, yl[k].get() + (size_t)ntp * M.ns, 6, ntp, ntp};
             P.push_back(q);
             O.push_back(o2);
         }
         tc_gemm(P, O, cx.err, nullptr, cx.st);
     }
     mixed_lu_factor(gl, cx);
-    // Z = G_s^{-1} G_c
-    std::vector<Rhs> zr;
-    for (sqbem_swimmer* s : sw) {
-        MixedSwimmer& M = s->mx;
-        const int nsp = M.G.n;
-        M.Z.alloc((size_t)nsp * 6, cx.st);
-        M.Z.zero();
-        M.Zh.alloc((size_t)nsp * 6, cx.st);
-        M.Zl.alloc((size_t)nsp * 6, cx.st);
-        cj.push_back(cp32_32(M.Gc.get(), M.ns, M.Z.get(), nsp, M.ns, 6));
-        Rhs r;
-        r.X = M.Z.get(); r.ldx = nsp; r.nrhs = 6; r.Sh = M.Zh.get(); r.Sl = M.Zl.get(); r.lds = nsp;
-        zr.push_back(r);
+    check_ctx(cx, "dgetrf (mixed Schur factor)");
+    std::vector<float*> inv;
+    for (size_t k = 0; k < G; ++k) {
+        MixedSwimmer& M = sw[k]->mx;
+        M.Gi.alloc((size_t)M.nsp * M.nsp, cx.st);
+        inv.push_back(M.Gi.get());
+    }
+    invert_group(gl, inv, {}, {}, cx);
+    // Z = G_s^{-1} G_c and S6 = F Z in FP64; S6 inverted on the host
+    std::vector<DevBuf<double>> gc64(G);
+    DevBuf<double> s6((size_t)36 * G, cx.st);
+    for (size_t k = 0; k < G; ++k) {
+        MixedSwimmer& M = sw[k]->mx;
+        gc64[k].alloc((size_t)M.ns * 6, cx.st);
+        cj.push_back(cp32_64(Gc[k].get(), M.ns, gc64[k].get(), M.ns, M.ns, 6));
+        M.Z64.alloc((size_t)M.ns * 6, cx.st);
+        mj.push_back(mv32(M.Gi.get(), M.nsp, M.ns, M.ns, gc64[k].get(), M.ns, 6, M.Z64.get(), M.ns, 1.0, 0.0));
     }
     copy_group(cj, cx.st);
     cj.clear();
-    mixed_lu_solve(gl, zr, cx);
-    // S6 = F Z in FP64, inverted on the host
-    DevBuf<double> s6((size_t)36 * sw.size(), cx.st);
-    for (size_t k = 0; k < sw.size(); ++k) {
+    matvec_group(mj, cx.st);
+    mj.clear();
+    for (size_t k = 0; k < G; ++k) {
         MixedSwimmer& M = sw[k]->mx;
-        M.Z64.alloc((size_t)M.ns * 6, cx.st);
-        cj.push_back(cp32_64(M.Z.get(), M.G.n, M.Z64.get(), M.ns, M.ns, 6));
         mj.push_back(mv64(M.F.get(), 6, 6, M.ns, M.Z64.get(), M.ns, 6, s6.get() + 36 * k, 6, 1.0, 0.0));
     }
-    copy_group(cj, cx.st);
     matvec_group(mj, cx.st);
-    std::vector<double> h6(36 * sw.size());
+    mj.clear();
+    std::vector<double> h6(36 * G);
     s6.download(h6.data(), h6.size());
-    check_ctx(cx, "dgetrf (mixed Schur factor)");
-    for (size_t k = 0; k < sw.size(); ++k) {
-        double inv[36];
-        if (!invert6(h6.data() + 36 * k, inv)) fail(SQBEM_ERR_SINGULAR, "dgesv failed (rigid-body 6 x 6 system)");
+    check_ctx(cx, "mixed Schur inverse");
+    for (size_t k = 0; k < G; ++k) {
+        double inv6[36];
+        if (!invert6(h6.data() + 36 * k, inv6)) fail(SQBEM_ERR_SINGULAR, "dgesv failed (rigid-body 6 x 6 system)");
         MixedSwimmer& M = sw[k]->mx;
         M.S6i.alloc(36, cx.st);
-        M.S6i.upload(inv, 36);
-    }
-    // the assembly-only buffers are no longer needed
-    for (sqbem_swimmer* s : sw) {
-        s->mx.Dh.release();
-        s->mx.Dl.release();
-        s->mx.Zh.release();
-        s->mx.Zl.release();
+        M.S6i.upload(inv6, 36);
     }
 }
 
@@ -341,9 +385,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     if (G == 0) return;
     const bool bounded = sw[0]->tube != nullptr;
     struct Work {
-        DevBuf<double> bt, bs, rt, rs, rc, rsp, yt64, v64, tmp6, dsw, dt, nrm;
-        DevBuf<float> yt32, v32;
-        DevBuf<bf16> yth, ytl, vh, vl;
+        DevBuf<double> bt, bs, rt, rs, rc, rsp, yt, tmp6, dsw, dt, nrm;
     };
     std::vector<Work> W(G);
     std::vector<MvJob> mj;
@@ -352,19 +394,11 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         MixedSwimmer& M = sw[k]->mx;
         Work& w = W[k];
         const int nt = M.nt, ns = M.ns, nc = M.nc;
-        const int ntp = bounded ? sw[k]->tube->mt.lu.n : 0, nsp = M.G.n;
         const size_t ntr = (size_t)std::max(nt, 1) * r;
-        w.bt.alloc(ntr, cx.st); w.rt.alloc(ntr, cx.st); w.dt.alloc(ntr, cx.st); w.yt64.alloc(ntr, cx.st);
-        w.bs.alloc((size_t)ns * r, cx.st); w.rs.alloc((size_t)ns * r, cx.st);
-        w.rsp.alloc((size_t)ns * r, cx.st); w.v64.alloc((size_t)ns * r, cx.st);
+        w.bt.alloc(ntr, cx.st); w.rt.alloc(ntr, cx.st); w.dt.alloc(ntr, cx.st); w.yt.alloc(ntr, cx.st);
+        w.bs.alloc((size_t)ns * r, cx.st); w.rs.alloc((size_t)ns * r, cx.st); w.rsp.alloc((size_t)ns * r, cx.st);
         w.rc.alloc((size_t)6 * r, cx.st); w.tmp6.alloc((size_t)6 * r, cx.st);
         w.dsw.alloc((size_t)nc * r, cx.st); w.nrm.alloc((size_t)4 * r, cx.st);
-        if (bounded) {
-            w.yt32.alloc((size_t)ntp * r, cx.st);
-            w.yth.alloc((size_t)ntp * r, cx.st);
-            w.ytl.alloc((size_t)ntp * r, cx.st);
-        }
-        w.v32.alloc((size_t)nsp * r, cx.st); w.vh.alloc((size_t)nsp * r, cx.st); w.vl.alloc((size_t)nsp * r, cx.st);
         CUDA_CHECK(cudaMemsetAsync(xs[k], 0, sizeof(double) * (size_t)(nt + nc) * r, cx.st));
         CUDA_CHECK(cudaMemsetAsync(w.rc.get(), 0, sizeof(double) * 6 * r, cx.st));
         if (prescribed) {
@@ -447,70 +481,33 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     for (size_t k = 0; k < G * r; ++k) worst = std::max(worst, r0[k] > 0 ? 1.0 : 0.0);
     for (it = 1; it <= REFINE_MAX_IT && worst > REFINE_TOL; ++it) {
         // (a) y_t = T^{-1} r_t   (b) r_s' = r_s - D y_t
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
+            if (bounded) {
+                const MixedTube& Tt = sw[k]->tube->mt;
+                mj.push_back(mv32(Tt.Ti.get(), Tt.ntp, M.nt, M.nt, W[k].rt.get(), M.nt, r, W[k].yt.get(), M.nt, 1.0, 0.0));
+            }
+        }
+        copy_group(cj, cx.st);
+        cj.clear();
+        matvec_group(mj, cx.st);
+        mj.clear();
         if (bounded) {
-            std::vector<MixedLU*> tl;
-            std::vector<Rhs> rh;
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                Work& w = W[k];
-                MixedLU& L = const_cast<sqbem_tube*>(sw[k]->tube)->mt.lu;
-                CUDA_CHECK(cudaMemsetAsync(w.yt32.get(), 0, sizeof(float) * (size_t)L.n * r, cx.st));
-                cj.push_back(cp64_32(w.rt.get(), M.nt, w.yt32.get(), L.n, M.nt, r));
-                tl.push_back(&L);
-                Rhs x;
-                x.X = w.yt32.get(); x.ldx = L.n; x.nrhs = r; x.Sh = w.yth.get(); x.Sl = w.ytl.get(); x.lds = L.n;
-                rh.push_back(x);
-            }
-            copy_group(cj, cx.st);
-            cj.clear();
-            mixed_lu_solve(tl, rh, cx);
-            for (size_t k = 0; k < G; ++k) {
-                MixedSwimmer& M = sw[k]->mx;
-                const int ntp = sw[k]->tube->mt.lu.n;
-                cj.push_back(cp32_64(W[k].yt32.get(), ntp, W[k].yt64.get(), M.nt, M.nt, r));
-                cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
-            }
-            copy_group(cj, cx.st);
-            cj.clear();
-            for (size_t k = 0; k < G; ++k) {
-                MixedSwimmer& M = sw[k]->mx;
-                mj.push_back(mv32(M.D.get(), M.ns, M.ns, M.nt, W[k].yt64.get(), M.nt, r, W[k].rsp.get(), M.ns, -1.0, 1.0));
+                mj.push_back(mv32(M.D.get(), M.ns, M.ns, M.nt, W[k].yt.get(), M.nt, r, W[k].rsp.get(), M.ns, -1.0, 1.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();
-        } else {
-            for (size_t k = 0; k < G; ++k) {
-                MixedSwimmer& M = sw[k]->mx;
-                cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
-            }
-            copy_group(cj, cx.st);
-            cj.clear();
         }
-        // (c) v = G_s^{-1} r_s'
-        {
-            std::vector<MixedLU*> gl;
-            std::vector<Rhs> rh;
-            for (size_t k = 0; k < G; ++k) {
-                MixedSwimmer& M = sw[k]->mx;
-                Work& w = W[k];
-                CUDA_CHECK(cudaMemsetAsync(w.v32.get(), 0, sizeof(float) * (size_t)M.G.n * r, cx.st));
-                cj.push_back(cp64_32(w.rsp.get(), M.ns, w.v32.get(), M.G.n, M.ns, r));
-                gl.push_back(&M.G);
-                Rhs x;
-                x.X = w.v32.get(); x.ldx = M.G.n; x.nrhs = r; x.Sh = w.vh.get(); x.Sl = w.vl.get(); x.lds = M.G.n;
-                rh.push_back(x);
-            }
-            copy_group(cj, cx.st);
-            cj.clear();
-            mixed_lu_solve(gl, rh, cx);
-            for (size_t k = 0; k < G; ++k) {
-                MixedSwimmer& M = sw[k]->mx;
-                cj.push_back(cp32_64(W[k].v32.get(), M.G.n, W[k].v64.get(), M.ns, M.ns, r));
-                cj.push_back(cp32_64(W[k].v32.get(), M.G.n, W[k].dsw.get(), M.nc, M.ns, r));
-            }
-            copy_group(cj, cx.st);
-            cj.clear();
+        // (c) v = G_s^{-1} r_s', written into the top of d_sw
+        for (size_t k = 0; k < G; ++k) {
+            MixedSwimmer& M = sw[k]->mx;
+            mj.push_back(mv32(M.Gi.get(), M.nsp, M.ns, M.ns, W[k].rsp.get(), M.ns, r, W[k].dsw.get(), M.nc, 1.0, 0.0));
         }
+        matvec_group(mj, cx.st);
+        mj.clear();
         if (prescribed) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
@@ -521,7 +518,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             // (d) dw = S6^{-1} (F v - r_c)   (e) ds = v - Z dw
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                mj.push_back(mv64(M.F.get(), 6, 6, M.ns, W[k].v64.get(), M.ns, r, W[k].tmp6.get(), 6, 1.0, 0.0));
+                mj.push_back(mv64(M.F.get(), 6, 6, M.ns, W[k].dsw.get(), M.nc, r, W[k].tmp6.get(), 6, 1.0, 0.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();
@@ -542,18 +539,17 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             matvec_group(mj, cx.st);
             mj.clear();
         }
-        // (f) dt = y_t - Y [ds; dw]   (g) x += d
+        // (f) d_t = y_t - Y [d_s; d_w]   (g) x += d
         if (bounded) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                cj.push_back(cp64(W[k].yt64.get(), M.nt, W[k].dt.get(), M.nt, M.nt, r));
+                cj.push_back(cp64(W[k].yt.get(), M.nt, W[k].dt.get(), M.nt, M.nt, r));
             }
             copy_group(cj, cx.st);
             cj.clear();
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                const int ntp = sw[k]->tube->mt.lu.n;
-                mj.push_back(mv32(M.Y.get(), ntp, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
+                mj.push_back(mv32(M.Y.get(), M.nt, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();

@@ -6,10 +6,12 @@
 //   [ 0  F  0  ] [ w ]   [ 0 ]        F: force-free / torque-free rows
 // Blocks are assembled in FP32 and kept for the FP64 residual.  The
 // preconditioner is the Schur elimination on split-BF16 tensor cores:
-// LU(T), Y = T^{-1}[B | Ct], G = [E | Cs] - D Y, LU(G_s), Z = G_s^{-1} G_c and
-// the 6 x 6 rigid-body system S6 = F Z solved in FP64.  Iterative refinement on
-// the full system, residuals accumulated in FP64, stops when the relative
-// residual reaches REFINE_TOL.
+// T^{-1} (LU of T, then the LU solve of the identity), Y = T^{-1}[B | Ct] as one
+// GEMM, G = [E | Cs] - D Y, G_s^{-1} the same way, Z = G_s^{-1} G_c and the
+// 6 x 6 rigid-body system S6 = F Z solved in FP64.  With the two inverses held
+// explicitly, every refinement step is a handful of HBM-bound products.
+// Iterative refinement on the full system, residuals accumulated in FP64,
+// stops when the relative residual reaches REFINE_TOL.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -24,28 +26,25 @@ constexpr double REFINE_TOL = 1e-11;
 constexpr int REFINE_MAX_IT = 30;
 
 struct MixedTube {
-    int nt = 0;
-    DevBuf<float> T;  // deflated T (nt x nt, column-major, ld nt), FP32
-    MixedLU lu;       // its factor (padded to a multiple of 128)
+    int nt = 0, ntp = 0;          // 3 Nt and its multiple of 128
+    DevBuf<float> T;              // deflated T (nt x nt, column-major, ld nt), FP32
+    DevBuf<float> Ti;             // T^{-1}, ntp x ntp column-major (padding: identity)
+    DevBuf<bf16> TiRh, TiRl;      // T^{-1} split row-major (left operand of Y = T^{-1}[B | Ct])
 };
 
 struct MixedSwimmer {
-    int ns = 0, nt = 0, nc = 0;       // 3 Ns, 3 Nt, 3 Ns + 6
-    DevBuf<float> B, AuBt;            // nt x ns
-    DevBuf<float> D;                  // ns x nt
-    DevBuf<float> E, AuBs;            // ns x ns
-    DevBuf<float> Ct, Cs;             // nt x 6, ns x 6
-    DevBuf<float> Y;                  // T^{-1} [B | Ct], ntp x nc (ld ntp)
-    DevBuf<bf16> Yh, Yl;              // its split column-major copy
-    DevBuf<bf16> Dh, Dl;              // D, split row-major (ld ntp, zero padding)
-    MixedLU G;                        // LU of G_s (padded)
-    DevBuf<float> Gc;                 // G_c, ns x 6
-    DevBuf<float> Z;                  // G_s^{-1} G_c, nsp x 6 (FP32)
-    DevBuf<bf16> Zh, Zl;
-    DevBuf<double> Z64;               // Z in FP64 (ns x 6)
-    DevBuf<double> F;                 // 6 x ns, column-major (ld 6), unscaled
-    DevBuf<double> S6i;               // (F Z)^{-1}, 6 x 6 column-major
-    DevBuf<double> K;                 // rigid-body map, ns x 6
+    int ns = 0, nt = 0, nc = 0;   // 3 Ns, 3 Nt, 3 Ns + 6
+    int nsp = 0;                  // multiple of 128 >= ns
+    DevBuf<float> B, AuBt;        // nt x ns
+    DevBuf<float> D;              // ns x nt
+    DevBuf<float> E, AuBs;        // ns x ns
+    DevBuf<float> Ct, Cs;         // nt x 6, ns x 6
+    DevBuf<float> Y;              // T^{-1} [B | Ct], nt x nc (ld nt)
+    DevBuf<float> Gi;             // G_s^{-1}, nsp x nsp column-major
+    DevBuf<double> Z64;           // G_s^{-1} G_c (ns x 6), FP64
+    DevBuf<double> F;             // 6 x ns, column-major (ld 6), unscaled
+    DevBuf<double> S6i;           // (F Z)^{-1}, 6 x 6 column-major
+    DevBuf<double> K;             // rigid-body map, ns x 6
 };
 
 }  // namespace sqbem

@@ -27,6 +27,18 @@ std::mutex g_mu;
 std::atomic<bool> g_on{false};
 std::vector<Pending> g_pending;
 std::map<std::string, Agg> g_agg;
+std::vector<cudaEvent_t> g_free;  // recorded-and-collected events, reused
+
+cudaEvent_t take_event() {
+    if (!g_free.empty()) {
+        cudaEvent_t e = g_free.back();
+        g_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    CUDA_CHECK(cudaEventCreate(&e));
+    return e;
+}
 
 void collect_locked() {
     for (auto& p : g_pending) {
@@ -41,8 +53,8 @@ void collect_locked() {
                 g.bytes += p.bytes;
             }
         }
-        if (p.a) cudaEventDestroy(p.a);
-        if (p.b) cudaEventDestroy(p.b);
+        if (p.a) g_free.push_back(p.a);
+        if (p.b) g_free.push_back(p.b);
     }
     g_pending.clear();
 }
@@ -53,8 +65,8 @@ bool kstats_on() { return g_on.load(std::memory_order_relaxed); }
 int kstat_begin(cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_mu);
     Pending p;
-    CUDA_CHECK(cudaEventCreate(&p.a));
-    CUDA_CHECK(cudaEventCreate(&p.b));
+    p.a = take_event();
+    p.b = take_event();
     CUDA_CHECK(cudaEventRecord(p.a, st));
     g_pending.push_back(p);
     return (int)g_pending.size() - 1;

@@ -142,7 +142,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // Problems of one launch travel as a __grid_constant__ kernel parameter (TMA
 // reads the tensor maps straight from parameter space; no device copies, so a
 // launch can be captured into a CUDA graph).
-constexpr int MAXP = 24;
+#ifndef SQBEM_TC_MAXP
+#define SQBEM_TC_MAXP 48
+#endif
+constexpr int MAXP = SQBEM_TC_MAXP;
 struct KArgs {
     int nprob;
     int total_tiles;
@@ -289,37 +292,95 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             const int tm = local / P.tiles_n, tn = local % P.tiles_n;
             if (!mbar_wait(tfull0 + 8 * acc, aph, err)) break;
             tc_fence_after();
+            // the problem's fields once per tile, in registers (parameter-space reads
+            // inside the element loop cost ~30 cycles each)
             const int m = tm * BM + row;
             const bool row_ok = m < P.M;
+            const int N = P.N;
+            const float alpha = P.alpha, beta = P.beta;
+            const bool chk = P.check_unit != 0;
+            float* const Cp = P.C;
+            const long long crs = P.c_rs, ccs = P.c_cs;
+            bf16* const Oh = P.O_hi;
+            bf16* const Ol = P.O_lo;
+            const long long ors = P.o_rs, ocs = P.o_cs;
+            bf16* const Ph = P.P_hi;
+            bf16* const Pl = P.P_lo;
+            const long long prs = P.p_rs, pcs = P.p_cs;
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
                 tmem_ld32(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * BN + c0), v);
-                if (!row_ok) continue;
+                const int n0 = tn * BN + c0;
+                const int cnt = min(32, N - n0);
+                if (!row_ok || cnt <= 0) continue;
+                if (Cp) {
+                    float* const c = Cp + (long long)m * crs + (long long)n0 * ccs;
+                    if (ccs == 1 && cnt == 32 && ((uintptr_t)c & 15) == 0) {
+                        // this thread's 32 columns are contiguous (row-major C)
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int n = tn * BN + c0 + j;
-                    if (n >= P.N) break;
-                    float x = P.alpha * v[j];
-                    if (P.C) {
-                        float* c = P.C + (long long)m * P.c_rs + (long long)n * P.c_cs;
-                        if (P.beta != 0.f) x = fmaf(P.beta, *c, x);
-                        *c = x;
+                        for (int j = 0; j < 32; j += 4) {
+                            float4 y = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
+                            if (beta != 0.f) {
+                                const float4 o = *reinterpret_cast<const float4*>(c + j);
+                                y.x = fmaf(beta, o.x, y.x); y.y = fmaf(beta, o.y, y.y);
+                                y.z = fmaf(beta, o.z, y.z); y.w = fmaf(beta, o.w, y.w);
+                            }
+                            *reinterpret_cast<float4*>(c + j) = y;
+                            v[j] = y.x; v[j + 1] = y.y; v[j + 2] = y.z; v[j + 3] = y.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (j >= cnt) break;
+                            float x = alpha * v[j];
+                            float* const cj = c + (long long)j * ccs;
+                            if (beta != 0.f) x = fmaf(beta, *cj, x);
+                            *cj = x;
+                            v[j] = x;
+                        }
                     }
-                    if (P.check_unit && !(fabsf(x) <= 1.f)) any_big = 1;
-                    if (P.O_hi) {
-                        const bf16 h = __float2bfloat16_rn(x);
-                        const bf16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-                        const long long o = (long long)m * P.o_rs + (long long)n * P.o_cs;
-                        P.O_hi[o] = h;
-                        P.O_lo[o] = l;
-                    }
-                    if (P.P_hi) {
-                        const bf16 h = __float2bfloat16_rn(x);
-                        const bf16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-                        const long long o = (long long)m * P.p_rs + (long long)n * P.p_cs;
-                        P.P_hi[o] = h;
-                        P.P_lo[o] = l;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) v[j] *= alpha;
+                }
+                if (chk)
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (j < cnt && !(fabsf(v[j]) <= 1.f)) any_big = 1;
+                // split outputs: 16-byte vectors where the thread's columns are contiguous
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    bf16* const H = w == 0 ? Oh : Ph;
+                    bf16* const Lo = w == 0 ? Ol : Pl;
+                    if (!H) continue;
+                    const long long rs = w == 0 ? ors : prs, cs = w == 0 ? ocs : pcs;
+                    const long long base = (long long)m * rs + (long long)n0 * cs;
+                    if (cs == 1 && cnt == 32 && ((base & 7) == 0) && (((uintptr_t)H & 15) == 0) &&
+                        (((uintptr_t)Lo & 15) == 0)) {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 8) {
+                            uint4 hv, lv;
+                            bf16* hp = reinterpret_cast<bf16*>(&hv);
+                            bf16* lp = reinterpret_cast<bf16*>(&lv);
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const bf16 h = __float2bfloat16_rn(v[j + q]);
+                                hp[q] = h;
+                                lp[q] = __float2bfloat16_rn(v[j + q] - __bfloat162float(h));
+                            }
+                            *reinterpret_cast<uint4*>(H + base + j) = hv;
+                            *reinterpret_cast<uint4*>(Lo + base + j) = lv;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (j >= cnt) break;
+                            const bf16 h = __float2bfloat16_rn(v[j]);
+                            const long long o = base + (long long)j * cs;
+                            H[o] = h;
+                            Lo[o] = __float2bfloat16_rn(v[j] - __bfloat162float(h));
+                        }
                     }
                 }
             }
@@ -436,7 +497,8 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
         a.maps[4 * a.nprob + 2] = make_map(o.B.hi, P.N, P.K, o.B.ld);
         a.maps[4 * a.nprob + 3] = make_map(o.B.lo, P.N, P.K, o.B.ld);
         a.probs[a.nprob++] = P;
-        flops += 2.0 * P.M * P.N * P.K;
+        // tensor-pipe work: three BF16 products (hi*hi, hi*lo, lo*hi) per element product
+        flops += 3.0 * 2.0 * P.M * P.N * P.K;
         bytes += 4.0 * ((double)P.M * P.K + (double)P.K * P.N) + 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
     }
     flush(flops, bytes);
