@@ -112,6 +112,24 @@ int sqbem_gemm_mixed(int M, int N, int K, float alpha, const float* A, int lda, 
 int sqbem_velocity_at(int P, const double* V, const double* u, const double* f, double mu, int npts,
                       const double* pts, double* out, int precision);
 
+/* velocity_at without device allocation.  No counterpart in the reference.
+ * For callers that cannot allocate device memory themselves -- e.g. a host
+ * framework that owns all device memory in a pre-reserved arena and forbids
+ * allocations inside its time loop.  Same result as sqbem_velocity_at, but
+ * V (9 per panel), u, f (3 per panel), pts and out (3 per point) are DEVICE
+ * pointers owned by the caller, and stream is a cudaStream_t (NULL: the
+ * default stream).  The per-panel records and the overflow flag the kernels
+ * need live in a file-scope device array for at most
+ * SQBEM_NOALLOC_MAX_PANELS panels (2.3 MB, held by every GPU that loads the
+ * library until the process exits); larger P is rejected with SQBEM_ERR_ARG.
+ * The array's device address is looked up on the first call on each device,
+ * so make that first call before any stream capture.  Every call shares the
+ * array and overwrites it: calls that overlap on the GPU race.  The call
+ * returns after its work on `stream` has completed. */
+#define SQBEM_NOALLOC_MAX_PANELS 16384
+int sqbem_velocity_at_noalloc(int P, const double* V, const double* u, const double* f, double mu, int npts,
+                              const double* pts, double* out, int precision, void* stream);
+
 /* ---------------------------------------------------------------- tube
  * Tube, src/swimmer.hpp:33-75: swimmer_tube_mesh + assembly of the tube-tube
  * single-layer block T (3Nt x 3Nt) + Wielandt deflation + LU, all on the GPU.

@@ -51,6 +51,7 @@ SIGNATURES = {
     "sqbem_panel_integrals": (_c_i, [_c_i, _D, _D, _I, _D, _D]),
     "sqbem_solve_dense": (_c_i, [_c_i, _c_i, _D, _D, _I]),
     "sqbem_velocity_at": (_c_i, [_c_i, _D, _D, _D, _c_d, _c_i, _D, _D, _c_i]),
+    "sqbem_velocity_at_noalloc": (_c_i, [_c_i, _VP, _VP, _VP, _c_d, _c_i, _VP, _VP, _c_i, _VP]),
     "sqbem_tube_create": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _c_d, _c_i, ctypes.POINTER(_VP)]),
     "sqbem_tube_panels": (_c_i, [_VP, _I]),
     "sqbem_tube_mesh_get": (_c_i, [_VP, _D, _I]),
