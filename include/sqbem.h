@@ -202,6 +202,48 @@ typedef struct {
 int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
                            double* device_seconds);
 
+/* ---------------------------------------------------------------- trajectories
+ * TrajectoryParams, src/trajectory.hpp:23-36 (same fields, same defaults when
+ * filled by sqbem_trajectory_defaults). */
+typedef struct {
+    double alpha;       /* B2/B1 (pusher < 0 < puller) */
+    double a_over_R;    /* confinement */
+    double beta0;       /* initial offset from the axis, in units of (R - a) */
+    double pitch0_deg;  /* initial tilt toward +x */
+    double yaw0_deg;    /* initial tilt toward +y */
+    double dt;          /* time step, units a/B1 */
+    double t_max;
+    double L_over_R;    /* truncated tube length */
+    int n_theta;        /* tube panels around the circumference */
+    int sphere_level;   /* icosphere refinement */
+    double beta_stop;   /* stop when beta exceeds this (wall contact) */
+    double budget_s;    /* wall-clock budget per call, 0 = unlimited */
+} sqbem_traj_params;
+
+int sqbem_trajectory_defaults(sqbem_traj_params* p);
+
+/* run_trajectory, src/trajectory.hpp:42-151: integrates (or resumes) one
+ * trajectory -- 3 RK4 start-up steps then 4th-order Adams-Bashforth, |e|
+ * renormalised -- rebuilding only the swimmer couplings each evaluation against
+ * the tube factored once.  Writes <out_prefix>.csv (t, x, y, z, ex, ey, ez, Ux,
+ * Uy, Uz, Omx, Omy, Omz, beta; 10 significant digits) and keeps
+ * <out_prefix>.ckpt (17 digits) for restart, in the reference's formats.
+ * status receives "finished", "wall contact" or "paused". */
+int sqbem_run_trajectory(const sqbem_traj_params* p, const char* out_prefix, int verbose, int precision,
+                         char* status, int status_cap);
+
+/* Ensemble of n swimmers in one tube (a_over_R, L_over_R, n_theta and
+ * sphere_level from *p), advanced together: every time-stepping stage
+ * evaluates all active swimmers with grouped launches.  y0: n x 6 initial
+ * states (x, y, z, ex, ey, ez); alpha: n values of B2/B1.  scheme 0 = the
+ * reference's RK4 start-up + AB4, 1 = classical RK4 every step.  Outputs:
+ * states (n x (steps + 1) x 6), U and Om (n x steps x 3, at the start of each
+ * step), status (n: 0 running / finished, 1 wall contact; a swimmer past
+ * p->beta_stop is frozen).  *device_seconds (may be NULL): GPU time. */
+int sqbem_trajectory_ensemble(int n, const double* y0, const double* alpha, const sqbem_traj_params* p,
+                              int steps, int scheme, int precision, double* states, double* U, double* Om,
+                              int* status, double* device_seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,9 @@ SIGNATURES = {
     "sqbem_kernel_stats": (_c_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), _D, _D, _D]),
     "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
     "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
+    "sqbem_trajectory_defaults": (_c_i, [_VP]),
+    "sqbem_run_trajectory": (_c_i, [_VP, ctypes.c_char_p, _c_i, _c_i, ctypes.c_char_p, _c_i]),
+    "sqbem_trajectory_ensemble": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _D, _D, _D, _I, _D]),
     "sqbem_gemm_mixed": (_c_i, [_c_i, _c_i, _c_i, ctypes.c_float, ctypes.POINTER(ctypes.c_float), _c_i,
                                 ctypes.POINTER(ctypes.c_float), _c_i, ctypes.c_float,
                                 ctypes.POINTER(ctypes.c_float), _c_i]),
@@ -90,6 +93,45 @@ def gemm_mixed(A, B, C=None, alpha=1.0, beta=0.0):
     _check(lib().sqbem_gemm_mixed(M, N, K, alpha, A.ctypes.data_as(fp), M, B.ctypes.data_as(fp), K, beta,
                                   Cm.ctypes.data_as(fp), M))
     return Cm
+
+
+class TrajParams(ctypes.Structure):
+    """sqbem_traj_params = TrajectoryParams (src/trajectory.hpp:23-36)."""
+    _fields_ = [("alpha", ctypes.c_double), ("a_over_R", ctypes.c_double), ("beta0", ctypes.c_double),
+                ("pitch0_deg", ctypes.c_double), ("yaw0_deg", ctypes.c_double), ("dt", ctypes.c_double),
+                ("t_max", ctypes.c_double), ("L_over_R", ctypes.c_double), ("n_theta", ctypes.c_int),
+                ("sphere_level", ctypes.c_int), ("beta_stop", ctypes.c_double), ("budget_s", ctypes.c_double)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        _check(lib().sqbem_trajectory_defaults(ctypes.byref(self)))
+        for k, v in kw.items():
+            if k not in dict(self._fields_):
+                raise KeyError(k)
+            setattr(self, k, v)
+
+
+def run_trajectory(P, out_prefix, verbose=False, precision=FP64):
+    """trajectory.hpp:42-151 on the GPU; writes <out_prefix>.csv / .ckpt, returns the status."""
+    buf = ctypes.create_string_buffer(64)
+    _check(lib().sqbem_run_trajectory(ctypes.byref(P), out_prefix.encode(), int(verbose), precision, buf, 64))
+    return buf.value.decode()
+
+
+def trajectory_ensemble(y0, alpha, P, steps, scheme=1, precision=MIXED):
+    """n swimmers in one tube: returns (states (n, steps+1, 6), U (n, steps, 3),
+    Om (n, steps, 3), status (n,), device seconds)."""
+    y0 = _f64(y0).reshape(-1, 6)
+    n = y0.shape[0]
+    al = _f64(np.broadcast_to(np.asarray(alpha, dtype=np.float64), (n,)))
+    states = np.zeros((n, steps + 1, 6))
+    U = np.zeros((n, steps, 3))
+    Om = np.zeros((n, steps, 3))
+    status = np.zeros(n, dtype=np.int32)
+    secs = ctypes.c_double(0)
+    _check(lib().sqbem_trajectory_ensemble(n, _dp(y0), _dp(al), ctypes.byref(P), steps, scheme, precision,
+                                           _dp(states), _dp(U), _dp(Om), _ip(status), ctypes.byref(secs)))
+    return states, U, Om, status, secs.value
 
 
 class Instance(ctypes.Structure):

@@ -1,0 +1,145 @@
+"""Trajectories (src/trajectory.hpp) on the GPU: the drop-in run_trajectory
+against the reference's own CSV, checkpoint / resume, and the batched ensemble
+against the oracle."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+sqbem = pytest.importorskip("sqbem")
+pytestmark = pytest.mark.gpu
+
+SMALL = dict(alpha=-1.5, a_over_R=0.3, beta0=0.5, pitch0_deg=5, yaw0_deg=10, dt=0.5, t_max=3.0, n_theta=12,
+             sphere_level=1)
+
+
+def read_csv(path):
+    lines = open(path).read().splitlines()
+    head = [l for l in lines if l.startswith("#") or l.startswith("t,")]
+    rows = np.array([[float(x) for x in l.split(",")] for l in lines if l and l[0] not in "#t"])
+    return head, rows
+
+
+def golden_rows():
+    g = golden("traj")
+    lines = [l for l in g["csv"].split("\n") if l]
+    head = [l for l in lines if l.startswith("#") or l.startswith("t,")]
+    rows = np.array([[float(x) for x in l.split(",")] for l in lines if l[0] not in "#t"])
+    return g["status"], head, rows
+
+
+def test_run_trajectory_fp64_matches_reference_csv(tmp_path):
+    status, head_ref, rows_ref = golden_rows()
+    prefix = str(tmp_path / "traj_small")
+    st = sqbem.run_trajectory(sqbem.TrajParams(**SMALL), prefix, precision=sqbem.FP64)
+    assert st == status
+    head, rows = read_csv(prefix + ".csv")
+    assert head == head_ref  # comment and header lines byte-identical
+    assert rows.shape == rows_ref.shape
+    np.testing.assert_allclose(rows, rows_ref, rtol=2e-9, atol=1e-12)  # 10 printed digits
+    assert not os.path.exists(prefix + ".ckpt")  # removed unless paused
+
+
+def test_run_trajectory_mixed_within_1e6(tmp_path):
+    _, _, rows_ref = golden_rows()
+    prefix = str(tmp_path / "traj_mixed")
+    sqbem.run_trajectory(sqbem.TrajParams(**SMALL), prefix, precision=sqbem.MIXED)
+    _, rows = read_csv(prefix + ".csv")
+    assert rows.shape == rows_ref.shape
+    err = np.max(np.abs(rows - rows_ref)) / np.max(np.abs(rows_ref))
+    assert err < 1e-6, err
+
+
+def test_pause_and_resume_from_checkpoint(tmp_path):
+    """budget_s tiny: the run pauses after its first step and keeps the
+    checkpoint; the second call resumes from it and finishes like one run."""
+    _, _, rows_ref = golden_rows()
+    prefix = str(tmp_path / "traj_resume")
+    st1 = sqbem.run_trajectory(sqbem.TrajParams(**SMALL, budget_s=1e-9), prefix, precision=sqbem.FP64)
+    assert st1 == "paused"
+    assert os.path.exists(prefix + ".ckpt")
+    t, step, nh = open(prefix + ".ckpt").readline().split()
+    assert float(t) == 0.5 and int(step) == 1 and int(nh) == 1
+    st2 = sqbem.run_trajectory(sqbem.TrajParams(**SMALL), prefix, precision=sqbem.FP64)
+    assert st2 == "finished"
+    _, rows = read_csv(prefix + ".csv")
+    np.testing.assert_allclose(rows, rows_ref, rtol=2e-9, atol=1e-12)
+
+
+def _initial_states(P, n, rng):
+    R = 1.0 / P.a_over_R
+    y0 = []
+    for k in range(n):
+        b = rng.uniform(0.1, 0.6) * (R - 1.0)
+        ph = rng.uniform(0, 2 * math.pi)
+        e = rng.normal(size=3)
+        e /= np.linalg.norm(e)
+        y0.append([b * math.cos(ph), b * math.sin(ph), 0.0, *e])
+    return np.array(y0)
+
+
+def test_ensemble_fp64_matches_oracle(oracle):
+    """three swimmers, the reference scheme (RK4 start-up + AB4), against the
+    oracle's evaluation loop"""
+    P = sqbem.TrajParams(a_over_R=0.3, dt=0.5, n_theta=8, sphere_level=1)
+    rng = np.random.default_rng(4)
+    y0 = _initial_states(P, 3, rng)
+    alpha = np.array([-2.0, 0.0, 3.0])
+    steps = 5
+    states, U, Om, status, _ = sqbem.trajectory_ensemble(y0, alpha, P, steps, scheme=0, precision=sqbem.FP64)
+    assert np.all(status == 0)
+    R = 1.0 / P.a_over_R
+    tube = oracle.Tube(R, 4 * R, 1.0, 8)
+    sph0 = oracle.icosphere(1.0, 1)
+
+    def evaluate(y, al):
+        c = np.array([y[0], y[1], 0.0])
+        e = np.array(y[3:6]) / np.linalg.norm(y[3:6])
+        S = sph0.copy()
+        S.translate(c)
+        s = oracle.SwimmerSolver(tube, S, c)
+        k = s.solve_free([s.slip(e, 1, 0), s.slip(e, 0, 1)])
+        u = k[0].U + al * k[1].U
+        w = k[0].Om + al * k[1].Om
+        return np.concatenate([u, np.cross(w, e)])
+
+    for m in range(3):
+        y = y0[m].copy()
+        hist = []
+        for s in range(steps):
+            d = evaluate(y, alpha[m])
+            if len(hist) < 3:
+                k2 = evaluate(y + 0.25 * d, alpha[m])
+                k3 = evaluate(y + 0.25 * k2, alpha[m])
+                k4 = evaluate(y + 0.5 * k3, alpha[m])
+                y = y + 0.5 / 6 * (d + 2 * k2 + 2 * k3 + k4)
+            else:
+                y = y + 0.5 / 24 * (55 * d - 59 * hist[2] + 37 * hist[1] - 9 * hist[0])
+            y[3:6] /= np.linalg.norm(y[3:6])
+            hist = (hist + [d])[-3:]
+            np.testing.assert_allclose(states[m, s + 1], y, rtol=1e-9, atol=1e-11)
+
+
+def test_ensemble_mixed_vs_fp64_rk4():
+    P = sqbem.TrajParams(a_over_R=0.3, dt=0.25, n_theta=10, sphere_level=1)
+    rng = np.random.default_rng(9)
+    y0 = _initial_states(P, 5, rng)
+    alpha = rng.uniform(-5, 5, 5)
+    s64, U64, _, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 4, scheme=1, precision=sqbem.FP64)
+    smx, Umx, _, _, t = sqbem.trajectory_ensemble(y0, alpha, P, 4, scheme=1, precision=sqbem.MIXED)
+    assert t > 0
+    assert np.max(np.abs(smx - s64)) < 1e-6 * np.max(np.abs(s64))
+    assert np.max(np.abs(Umx - U64)) < 1e-6 * np.max(np.abs(U64))
+
+
+def test_ensemble_wall_contact_freezes_member():
+    P = sqbem.TrajParams(a_over_R=0.3, dt=0.5, n_theta=8, sphere_level=1, beta_stop=0.5)
+    R = 1.0 / P.a_over_R
+    y0 = np.array([[0.6 * (R - 1.0), 0, 0, 0, 0, 1.0], [0.1 * (R - 1.0), 0, 0, 0, 0, 1.0]])
+    states, U, _, status, _ = sqbem.trajectory_ensemble(y0, [0.0, 0.0], P, 2, scheme=1, precision=sqbem.MIXED)
+    assert status[0] == 1 and status[1] == 0
+    np.testing.assert_array_equal(states[0, 2], y0[0])
+    assert np.all(np.isnan(U[0]))
