@@ -165,6 +165,17 @@ int sqbem_swimmer_timings(const sqbem_swimmer* s, double* t_assembly, double* t_
 /* refinement diagnostics of the last mixed-precision solve: iterations used and
  * the final relative FP64 residual (max over right-hand sides) */
 int sqbem_swimmer_refinement(const sqbem_swimmer* s, int* iterations, double* residual);
+/* Adjoint sensitivities (no counterpart in the reference, which has no
+ * derivatives; it differentiates the system of swimmer.hpp:107-139, 188-249):
+ * solve_free for nrhs slip fields plus, per right-hand side k, the derivatives
+ * of U and Omega with respect to a rigid translation c of the sphere (panels
+ * and centre together, slip field carried along), row-major 3 x 3 blocks
+ * dU_dc[9k + 3a + j] = dU_a/dc_j and dOm_dc likewise.  One transpose solve with
+ * the stored LU factors serves every right-hand side; the sphere-tube kernel
+ * derivatives are recomputed, not stored.  FP64 swimmers only
+ * (SQBEM_ERR_ARG otherwise). */
+int sqbem_swimmer_adjoint(sqbem_swimmer* s, int nrhs, const double* slips, double* U, double* Om,
+                          double* dU_dc, double* dOm_dc);
 void sqbem_swimmer_destroy(sqbem_swimmer* s);
 
 /* ---------------------------------------------------------------- duct flow
@@ -201,6 +212,15 @@ typedef struct {
 #define SQBEM_RESULT_STRIDE 16
 int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
                            double* device_seconds);
+
+/* Batched adjoint sensitivities: instance k as in sqbem_kinematics_batch
+ * (towed ignored), FP64 only.  results[k * SQBEM_ADJOINT_STRIDE + 24 m + ...]
+ * for the slip mode m (0: B1 = 1, 1: B2 = 1): U (3), Om (3), dU/dc (9,
+ * row-major [a][j]), dOm/dc (9).  For a squirmer B2/B1 = alpha, every quantity
+ * is mode 0 + alpha * mode 1, and d(U, Om)/d alpha is mode 1's (U, Om). */
+#define SQBEM_ADJOINT_STRIDE 48
+int sqbem_adjoint_batch(int n, const sqbem_instance* inst, int precision, double* results,
+                        double* device_seconds);
 
 /* ---------------------------------------------------------------- trajectories
  * TrajectoryParams, src/trajectory.hpp:23-36 (same fields, same defaults when

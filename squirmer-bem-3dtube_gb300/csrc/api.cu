@@ -354,6 +354,14 @@ extern "C" int sqbem_swimmer_solve_prescribed(sqbem_swimmer* s, const double* U,
     });
 }
 
+extern "C" int sqbem_swimmer_adjoint(sqbem_swimmer* s, int nrhs, const double* slips, double* U, double* Om,
+                                     double* dU_dc, double* dOm_dc) {
+    return guarded([&] {
+        if (!s || nrhs <= 0 || !slips || !U || !Om || !dU_dc || !dOm_dc) fail(SQBEM_ERR_ARG, "adjoint: bad arguments");
+        s->adjoint(nrhs, slips, U, Om, dU_dc, dOm_dc);
+    });
+}
+
 extern "C" int sqbem_swimmer_timings(const sqbem_swimmer* s, double* ta, double* ts) {
     return guarded([&] {
         if (!s) fail(SQBEM_ERR_ARG, "timings: null swimmer");

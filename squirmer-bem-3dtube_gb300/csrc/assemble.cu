@@ -591,3 +591,152 @@ void field_eval(const FieldJob& job, cudaStream_t st) {
 }
 
 }  // namespace sqbem
+
+// ---------------------------------------------------------------- adjoint contraction
+namespace sqbem {
+
+constexpr int ADJ_TT = 32;   // targets per CTA (one per lane)
+constexpr int ADJ_ST = 32;   // source panels per CTA (staged in shared memory)
+constexpr int ADJ_OUT = 6 * ADJ_MAX_MODES * 3;
+
+// Gradients with respect to r of  phi_G = lam.G(r).f = (lam.f)/|r| + (lam.r)(f.r)/|r|^3
+//   grad phi_G = [lam (f.r) + f (lam.r) - (lam.f) r] / |r|^3 - 3 (lam.r)(f.r) r / |r|^5
+// and of phi_T = lam.(T(r).m).v = -6 (r.m)(lam.r)(v.r) / |r|^5
+//   grad phi_T = -6 [m (lam.r)(v.r) + lam (r.m)(v.r) + v (r.m)(lam.r)] / |r|^5
+//                + 30 (r.m)(lam.r)(v.r) r / |r|^7
+// (kernels.hpp:8-9 differentiated), accumulated with the weights gs w, ts w.
+__global__ void __launch_bounds__(6 * ADJ_TT) adjoint_pairs_kernel(AdjTerm J, int nm, double* partial) {
+    __shared__ PanelRec sp[ADJ_ST];
+    __shared__ double sf[ADJ_ST][ADJ_MAX_MODES][3];
+    __shared__ double sv[ADJ_ST][ADJ_MAX_MODES][3];
+    const int tid = threadIdx.x, o = tid / ADJ_TT, lt = tid % ADJ_TT;
+    const int t = blockIdx.x * ADJ_TT + lt;
+    const int s0 = blockIdx.y * ADJ_ST, ns = min(ADJ_ST, J.nS - s0);
+    {
+        const double* srcd = reinterpret_cast<const double*>(J.src + s0);
+        double* dstd = reinterpret_cast<double*>(sp);
+        for (int e = tid; e < ns * 18; e += blockDim.x) dstd[e] = srcd[e];
+        for (int e = tid; e < ns * ADJ_MAX_MODES * 3; e += blockDim.x) {
+            const int s = e / (ADJ_MAX_MODES * 3), j = (e / 3) % ADJ_MAX_MODES, a = e % 3;
+            sf[s][j][a] = j < nm ? J.f[3 * (long long)(s0 + s) + a + j * J.f_ld] : 0.0;
+            sv[s][j][a] = (J.v_src && j < nm) ? J.v[3 * (long long)(s0 + s) + a + j * J.v_ld] : 0.0;
+        }
+    }
+    __syncthreads();
+    double acc[ADJ_MAX_MODES][3];
+#pragma unroll
+    for (int j = 0; j < ADJ_MAX_MODES; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.0;
+    if (t < J.nT) {
+        const double x = J.tgt[3 * t], y = J.tgt[3 * t + 1], z = J.tgt[3 * t + 2];
+        const double* lp = J.lam + 3 * (long long)t + o * J.lam_ld;
+        const double lx = lp[0], ly = lp[1], lz = lp[2];
+        double tv[ADJ_MAX_MODES][3];
+#pragma unroll
+        for (int j = 0; j < ADJ_MAX_MODES; ++j)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) tv[j][a] = (!J.v_src && j < nm) ? J.v[3 * (long long)t + a + j * J.v_ld] : 0.0;
+        for (int s = 0; s < ns; ++s) {
+            const PanelRec& P = sp[s];
+            const int rule = rule_of(P, x, y, z);
+            const double e0x = P.v[0] - x, e0y = P.v[1] - y, e0z = P.v[2] - z;
+            const double e1x = P.v[3] - x, e1y = P.v[4] - y, e1z = P.v[5] - z;
+            const double e2x = P.v[6] - x, e2y = P.v[7] - y, e2z = P.v[8] - z;
+            const double mx = P.n[0], my = P.n[1], mz = P.n[2];
+            double fv[ADJ_MAX_MODES][3], vv[ADJ_MAX_MODES][3], lf[ADJ_MAX_MODES];
+#pragma unroll
+            for (int j = 0; j < ADJ_MAX_MODES; ++j) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    fv[j][a] = sf[s][j][a];
+                    vv[j][a] = J.v_src ? sv[s][j][a] : tv[j][a];
+                }
+                lf[j] = lx * fv[j][0] + ly * fv[j][1] + lz * fv[j][2];
+            }
+            const int q0 = rule_off(rule), q1 = rule_off(rule + 1);
+            for (int q = q0; q < q1; ++q) {
+                const QPoint Q = d_rule[q];
+                const double rx = Q.l0 * e0x + Q.l1 * e1x + Q.l2 * e2x;
+                const double ry = Q.l0 * e0y + Q.l1 * e1y + Q.l2 * e2y;
+                const double rz = Q.l0 * e0z + Q.l1 * e1z + Q.l2 * e2z;
+                const double w = Q.w * P.area;
+                const double r2 = rx * rx + ry * ry + rz * rz;
+                const double ir = rsqrt(r2), ir2 = ir * ir, ir3 = ir * ir2, ir5 = ir3 * ir2, ir7 = ir5 * ir2;
+                const double sm = rx * mx + ry * my + rz * mz;
+                const double sl = rx * lx + ry * ly + rz * lz;
+                const double wg = w * J.gs, wt = w * J.ts;
+#pragma unroll
+                for (int j = 0; j < ADJ_MAX_MODES; ++j) {
+                    if (j >= nm) break;
+                    const double sfj = rx * fv[j][0] + ry * fv[j][1] + rz * fv[j][2];
+                    const double svj = rx * vv[j][0] + ry * vv[j][1] + rz * vv[j][2];
+                    // grad phi_G = (lam sf + f sl - lf r) ir3 + cg r
+                    const double cg = -3.0 * sl * sfj * ir5;
+                    // grad phi_T = -6 ir5 (m sl sv + lam sm sv + v sm sl) + ct r
+                    const double a1 = sl * svj, a2 = sm * svj, a3 = sm * sl;
+                    const double ct = 30.0 * a3 * svj * ir7, m6 = -6.0 * ir5;
+                    const double gx = (lx * sfj + fv[j][0] * sl - lf[j] * rx) * ir3 + cg * rx;
+                    const double gy = (ly * sfj + fv[j][1] * sl - lf[j] * ry) * ir3 + cg * ry;
+                    const double gz = (lz * sfj + fv[j][2] * sl - lf[j] * rz) * ir3 + cg * rz;
+                    const double tx = m6 * (mx * a1 + lx * a2 + vv[j][0] * a3) + ct * rx;
+                    const double ty = m6 * (my * a1 + ly * a2 + vv[j][1] * a3) + ct * ry;
+                    const double tz = m6 * (mz * a1 + lz * a2 + vv[j][2] * a3) + ct * rz;
+                    acc[j][0] += wg * gx + wt * tx;
+                    acc[j][1] += wg * gy + wt * ty;
+                    acc[j][2] += wg * gz + wt * tz;
+                }
+            }
+        }
+    }
+    // the 32 lanes of a warp share o: reduce over targets, lane 0 writes
+#pragma unroll
+    for (int j = 0; j < ADJ_MAX_MODES; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            double v = acc[j][a];
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+            acc[j][a] = v;
+        }
+    if (lt == 0) {
+        const long long cta = blockIdx.x + (long long)gridDim.x * blockIdx.y;
+        double* out = partial + cta * ADJ_OUT + o * ADJ_MAX_MODES * 3;
+#pragma unroll
+        for (int j = 0; j < ADJ_MAX_MODES; ++j)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) out[j * 3 + a] = acc[j][a];
+    }
+}
+
+// out[k] = sum over the ncta partial records, in order
+__global__ void adjoint_reduce_kernel(const double* __restrict__ partial, long long ncta, double* __restrict__ out) {
+    const int k = threadIdx.x;
+    if (k >= ADJ_OUT) return;
+    double s = 0.0;
+    for (long long c = 0; c < ncta; ++c) s += partial[c * ADJ_OUT + k];
+    out[k] = s;
+}
+
+void adjoint_pairs(const AdjTerm* terms, int nterms, int nm, double* out, cudaStream_t st) {
+    if (nm < 1 || nm > ADJ_MAX_MODES) fail(SQBEM_ERR_ARG, "adjoint_pairs: %d solutions (at most %d)", nm, ADJ_MAX_MODES);
+    init_tables();
+    long long total = 0;
+    for (int k = 0; k < nterms; ++k)
+        total += (long long)ceil_div(terms[k].nT, ADJ_TT) * ceil_div(terms[k].nS, ADJ_ST);
+    DevBuf<double> partial((size_t)std::max<long long>(total, 1) * ADJ_OUT, st);
+    partial.zero();
+    long long off = 0;
+    for (int k = 0; k < nterms; ++k) {
+        const AdjTerm& J = terms[k];
+        if (J.nT <= 0 || J.nS <= 0) continue;
+        const dim3 grid(ceil_div(J.nT, ADJ_TT), ceil_div(J.nS, ADJ_ST));
+        // far-rule estimate: per node and adjoint vector 54 + 81 nm flops
+        const double fl = (double)J.nT * J.nS * 7.0 * 6.0 * (54.0 + 81.0 * nm);
+        const double by = (double)J.nS * sizeof(PanelRec) * grid.x + (double)J.nT * 8.0 * 3.0 * 7.0;
+        TIMED_LAUNCH("adjoint_pairs", fl, by, adjoint_pairs_kernel, grid, 6 * ADJ_TT, 0, st, J, nm,
+                     partial.get() + off * ADJ_OUT);
+        off += (long long)grid.x * grid.y;
+    }
+    LAUNCH(adjoint_reduce_kernel, 1, 64, 0, st, partial.get(), total, out);
+}
+
+}  // namespace sqbem

@@ -66,3 +66,34 @@ void panel_pairs(int n, const PanelRec* P, const double* x0, const int* self, do
 void field_eval(const FieldJob& job, cudaStream_t st);
 
 }  // namespace sqbem
+
+namespace sqbem {
+
+// One sphere-tube coupling term of the adjoint contraction (adjoint.cu).  For a
+// rigid translation c of the sphere, every target x (3 per target) and every
+// source panel s contribute, per adjoint vector o < 6 and solution j < nm,
+//   gs * sum_q w_q grad_r [lam_o . G(r) f_j] + ts * sum_q w_q grad_r [lam_o . T(r).m_s v_j],
+// r = x_q - x, with the quadrature of the assembly (same rule choice).
+// lam[3t + a + o*lam_ld] belongs to target t; f[3s + a + j*f_ld] to source s;
+// v[3i + a + j*v_ld] to the sphere panel i, which is the source when v_src = 1
+// and the target otherwise.
+struct AdjTerm {
+    const double* tgt = nullptr;
+    int nT = 0;
+    const double* lam = nullptr;
+    long long lam_ld = 0;
+    const PanelRec* src = nullptr;
+    int nS = 0;
+    const double* f = nullptr;
+    long long f_ld = 0;
+    const double* v = nullptr;
+    long long v_ld = 0;
+    int v_src = 0;
+    double gs = 0, ts = 0;
+};
+constexpr int ADJ_MAX_MODES = 2;
+// out[o*6 + j*3 + k] (6 x ADJ_MAX_MODES x 3) <- sum over the terms; nm <= ADJ_MAX_MODES.
+// Deterministic: per-CTA partials reduced in a fixed order.
+void adjoint_pairs(const AdjTerm* terms, int nterms, int nm, double* out, cudaStream_t st);
+
+}  // namespace sqbem

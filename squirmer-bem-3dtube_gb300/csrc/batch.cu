@@ -255,3 +255,56 @@ extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int pre
         if (device_seconds) *device_seconds = secs;
     });
 }
+
+// Adjoint sensitivities per instance: build (FP64), both slip modes, and the
+// translation derivatives of (U, Omega) for each (adjoint.cu).
+extern "C" int sqbem_adjoint_batch(int n, const sqbem_instance* inst, int precision, double* results,
+                                   double* device_seconds) {
+    return guarded([&] {
+        if (n < 0 || (n > 0 && (!inst || !results)) || precision != SQBEM_FP64)
+            fail(SQBEM_ERR_ARG, "adjoint_batch: bad arguments (FP64 only)");
+        for (int k = 0; k < n; ++k) validate(inst[k]);
+        if (device_seconds) *device_seconds = 0;
+        if (n == 0) return;
+        require_device();
+        Stream bs;
+        EventTimer clk;
+        clk.start(bs);
+        for (int k = 0; k < n; ++k) {
+            const Prepared P = prepare(inst[k]);
+            std::unique_ptr<sqbem_tube> t;
+            if (P.bounded) {
+                t = std::make_unique<sqbem_tube>();
+                t->st.borrow(bs);
+                t->R = P.R; t->L = P.L; t->a = 1.0; t->n_theta = inst[k].n_theta; t->n_r = inst[k].n_r; t->mu = 1.0;
+                t->precision = SQBEM_FP64;
+                t->mesh = P.tube;
+                t->build_device();
+            }
+            sqbem_swimmer s;
+            s.st.borrow(bs);
+            const double c[3] = {P.b, 0, 0};
+            s.build(t.get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_FP64);
+            auto slips = squirmer_slip_host(s.host_panels, c, inst[k].e, 1, 0);
+            const auto u2 = squirmer_slip_host(s.host_panels, c, inst[k].e, 0, 1);
+            slips.insert(slips.end(), u2.begin(), u2.end());
+            double U[6], Om[6], dU[18], dOm[18];
+            s.adjoint(2, slips.data(), U, Om, dU, dOm);
+            double* r = results + (size_t)k * SQBEM_ADJOINT_STRIDE;
+            for (int m = 0; m < 2; ++m) {
+                double* o = r + 24 * m;
+                for (int a = 0; a < 3; ++a) {
+                    o[a] = U[3 * m + a];
+                    o[3 + a] = Om[3 * m + a];
+                }
+                for (int e = 0; e < 9; ++e) {
+                    o[6 + e] = dU[9 * m + e];
+                    o[15 + e] = dOm[9 * m + e];
+                }
+            }
+        }
+        clk.stop(bs);
+        const double secs = clk.seconds();
+        if (device_seconds) *device_seconds = secs;
+    });
+}

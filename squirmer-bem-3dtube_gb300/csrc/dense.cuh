@@ -48,6 +48,8 @@ struct LU64 {
     void factor_inplace(DevBuf<double>&& M, int n, cudaStream_t st, const char* what);
     // B <- A^{-1} B for B (n x nrhs, leading dimension ldb, device)
     void solve(double* B, long long ldb, int nrhs, cudaStream_t st) const;
+    // B <- A^{-T} B (dgetrs 'T'): U^T then L^T solves, then the row exchanges undone
+    void solve_transpose(double* B, long long ldb, int nrhs, cudaStream_t st) const;
 };
 
 // Solve with the certified LU; helpers shared with the mixed path.

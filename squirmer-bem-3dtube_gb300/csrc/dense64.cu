@@ -396,3 +396,49 @@ void LU64::solve(double* B, long long ldb, int nrhs, cudaStream_t st) const {
 }
 
 }  // namespace sqbem
+
+namespace sqbem {
+
+// B <- P^T applied in reverse exchange order (undoes laswp)
+__global__ void laswp_reverse_kernel(double* B, long long ldb, int n, int nrhs, const int* ipiv) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nrhs) return;
+    for (int j = n - 1; j >= 0; --j) {
+        const int p = ipiv[j];
+        if (p != j) {
+            const double t = B[j + c * ldb];
+            B[j + c * ldb] = B[p + c * ldb];
+            B[p + c * ldb] = t;
+        }
+    }
+}
+
+// A^T X = B with P A = L U:  A^T = U^T L^T P, so X = P^T L^{-T} U^{-T} B.
+// U^T is lower triangular (forward, block inverses transposed), L^T unit upper
+// (backward); the off-diagonal blocks enter as transposed GEMM operands.
+void LU64::solve_transpose(double* B, long long ldb, int nrhs, cudaStream_t st) const {
+    if (nrhs <= 0 || n == 0) return;
+    DevBuf<double> work((size_t)LU_NB * nrhs, st);
+    double* W = work.get();
+    const int nblk = ceil_div(n, LU_NB);
+    for (int b = 0; b < nblk; ++b) {  // forward with U^T
+        const int k0 = b * LU_NB, kb = std::min(LU_NB, n - k0);
+        if (k0 > 0)  // B_k -= (U_{0:k0, k})^T X_{0:k0}
+            gemm64(true, false, kb, nrhs, k0, -1.0, A.get() + k0 * ld, ld, B, ldb, 1.0, B + k0, ldb, st);
+        gemm64(true, false, kb, nrhs, kb, 1.0, Uinv.get() + (long long)b * LU_NB * LU_NB, LU_NB, B + k0, ldb, 0.0, W,
+               kb, st);
+        copy_matrix64(W, kb, B + k0, ldb, kb, nrhs, st);
+    }
+    for (int b = nblk - 1; b >= 0; --b) {  // backward with L^T (unit)
+        const int k0 = b * LU_NB, kb = std::min(LU_NB, n - k0);
+        if (k0 + kb < n)  // B_k -= (L_{k0+kb:n, k})^T X_{k0+kb:n}
+            gemm64(true, false, kb, nrhs, n - k0 - kb, -1.0, A.get() + (k0 + kb) + k0 * ld, ld, B + k0 + kb, ldb, 1.0,
+                   B + k0, ldb, st);
+        gemm64(true, false, kb, nrhs, kb, 1.0, Linv.get() + (long long)b * LU_NB * LU_NB, LU_NB, B + k0, ldb, 0.0, W,
+               kb, st);
+        copy_matrix64(W, kb, B + k0, ldb, kb, nrhs, st);
+    }
+    if (pivoted) LAUNCH(laswp_reverse_kernel, ceil_div(nrhs, 128), 128, 0, st, B, ldb, n, nrhs, ipiv.get());
+}
+
+}  // namespace sqbem

@@ -182,6 +182,28 @@ void sqbem_swimmer::build_fp64() {
     t_schur = clock2.seconds();
 }
 
+void sqbem_swimmer::factor_M() {
+    if (haveM) return;
+    const int ns = 3 * Ns, n = ns + 6;
+    // M = [Gs | Gc ; scaled force/torque rows | 0]   (swimmer.hpp:108-125)
+    DevBuf<double> M((size_t)n * n, st);
+    M.zero();
+    copy_matrix64(Gs.get(), ns, M.get(), n, ns, ns, st);
+    copy_matrix64(Gc.get(), ns, M.get() + (size_t)n * ns, n, ns, 6, st);
+    DevBuf<double> amax(1, st);
+    max_abs64(Gs.get(), ns, ns, ns, amax.get(), st);
+    double h_amax = 0;
+    amax.download(&h_amax, 1);
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    const double sc = h_amax / panels.area_max;
+    const auto F = constraint_rows(host_panels, xc, sc);
+    count_h2d(F.size() * sizeof(double));
+    CUDA_CHECK(cudaMemcpy2DAsync(M.get() + ns, sizeof(double) * n, F.data(), sizeof(double) * 6, sizeof(double) * 6,
+                                 ns, cudaMemcpyHostToDevice, st));
+    luM.factor_inplace(std::move(M), n, st, "dgesv failed");
+    haveM = true;
+}
+
 void sqbem_swimmer::solve_free(int nrhs, const double* slips, double* U, double* Om, double* f_sphere,
                                double* f_tube) {
     const int ns = 3 * Ns, nt = 3 * Nt, n = ns + 6;
@@ -189,25 +211,7 @@ void sqbem_swimmer::solve_free(int nrhs, const double* slips, double* U, double*
         solve_mixed(false, nrhs, slips, U, Om, f_sphere, f_tube);
         return;
     }
-    if (!haveM) {
-        // M = [Gs | Gc ; scaled force/torque rows | 0]   (swimmer.hpp:108-125)
-        DevBuf<double> M((size_t)n * n, st);
-        M.zero();
-        copy_matrix64(Gs.get(), ns, M.get(), n, ns, ns, st);
-        copy_matrix64(Gc.get(), ns, M.get() + (size_t)n * ns, n, ns, 6, st);
-        DevBuf<double> amax(1, st);
-        max_abs64(Gs.get(), ns, ns, ns, amax.get(), st);
-        double h_amax = 0;
-        amax.download(&h_amax, 1);
-        CUDA_CHECK(cudaStreamSynchronize(st));
-        const double sc = h_amax / panels.area_max;
-        const auto F = constraint_rows(host_panels, xc, sc);
-        count_h2d(F.size() * sizeof(double));
-        CUDA_CHECK(cudaMemcpy2DAsync(M.get() + ns, sizeof(double) * n, F.data(), sizeof(double) * 6, sizeof(double) * 6,
-                                     ns, cudaMemcpyHostToDevice, st));
-        luM.factor_inplace(std::move(M), n, st, "dgesv failed");
-        haveM = true;
-    }
+    factor_M();
     // reduced right-hand sides (swimmer.hpp:256-269)
     DevBuf<double> u((size_t)ns * nrhs, st), Rh((size_t)n * nrhs, st), rt;
     u.upload(slips, (size_t)ns * nrhs);

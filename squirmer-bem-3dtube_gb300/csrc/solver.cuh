@@ -110,10 +110,14 @@ struct sqbem_swimmer {
     void set_geometry(const sqbem_tube* tube, int Ns, const double* V, const double* center, double mu,
                       int precision);
     void build_fp64();
+    void factor_M();  // LU of M = [Gs Gc; F 0] (FP64 path), once
     void solve_free(int nrhs, const double* slips, double* U, double* Om, double* f_sphere, double* f_tube);
     void solve_prescribed(const double* U, const double* Om, double* f_sphere, double* f_tube);
     void solve_mixed(bool prescribed, int nrhs, const double* in, double* U, double* Om, double* f_sphere,
                      double* f_tube);
+    // free-swimming solutions and their derivatives with respect to a rigid
+    // translation of the sphere (adjoint.cu); per right-hand side 3 + 3 + 9 + 9
+    void adjoint(int nrhs, const double* slips, double* U, double* Om, double* dU_dc, double* dOm_dc);
 };
 
 // DuctFlow, src/duct_flow.hpp:22-109

@@ -61,6 +61,7 @@ SIGNATURES = {
     "sqbem_swimmer_solve_prescribed": (_c_i, [_VP, _D, _D, _D, _D]),
     "sqbem_swimmer_timings": (_c_i, [_VP, _D, _D]),
     "sqbem_swimmer_refinement": (_c_i, [_VP, _I, _D]),
+    "sqbem_swimmer_adjoint": (_c_i, [_VP, _c_i, _D, _D, _D, _D, _D]),
     "sqbem_swimmer_destroy": (None, [_VP]),
     "sqbem_duct_create": (_c_i, [_c_d, _c_d, _c_i, _c_i, _c_i, _c_d, _c_i, ctypes.POINTER(_VP)]),
     "sqbem_duct_panels": (_c_i, [_VP, _I]),
@@ -72,6 +73,7 @@ SIGNATURES = {
     "sqbem_kernel_stats": (_c_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), _D, _D, _D]),
     "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
     "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
+    "sqbem_adjoint_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
     "sqbem_trajectory_defaults": (_c_i, [_VP]),
     "sqbem_run_trajectory": (_c_i, [_VP, ctypes.c_char_p, _c_i, _c_i, ctypes.c_char_p, _c_i]),
     "sqbem_trajectory_ensemble": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _D, _D, _D, _I, _D]),
@@ -142,6 +144,7 @@ class Instance(ctypes.Structure):
 
 
 RESULT_STRIDE = 16
+ADJOINT_STRIDE = 48
 
 _LIB = None
 
@@ -209,10 +212,7 @@ def kernel_stats_classes():
     return [c for c in buf.value.decode().split(",") if c]
 
 
-def kinematics_batch(instances, precision=MIXED):
-    """sqbem_kinematics_batch: instances = list of dicts with a_over_R, beta,
-    L_over_R, e, n_theta, n_r, sphere_level, towed.  Returns (results
-    (n x RESULT_STRIDE), device seconds)."""
+def _instances(instances):
     n = len(instances)
     arr = (Instance * n)()
     for k, d in enumerate(instances):
@@ -226,10 +226,35 @@ def kinematics_batch(instances, precision=MIXED):
         arr[k].n_r = d.get("n_r", 4)
         arr[k].sphere_level = d["sphere_level"]
         arr[k].towed = int(d.get("towed", 0))
+    return arr
+
+
+def kinematics_batch(instances, precision=MIXED):
+    """sqbem_kinematics_batch: instances = list of dicts with a_over_R, beta,
+    L_over_R, e, n_theta, n_r, sphere_level, towed.  Returns (results
+    (n x RESULT_STRIDE), device seconds)."""
+    n = len(instances)
+    arr = _instances(instances)
     res = np.zeros((n, RESULT_STRIDE))
     secs = ctypes.c_double(0)
     _check(lib().sqbem_kinematics_batch(n, ctypes.cast(arr, _VP), precision, _dp(res), ctypes.byref(secs)))
     return res, secs.value
+
+
+def adjoint_batch(instances, precision=FP64):
+    """sqbem_adjoint_batch: per instance and slip mode m (0: B1, 1: B2) the
+    free-swimming U, Om and their derivatives with respect to the sphere centre.
+    Returns (dict of arrays U (n, 2, 3), Om (n, 2, 3), dU_dc (n, 2, 3, 3),
+    dOm_dc (n, 2, 3, 3); device seconds)."""
+    n = len(instances)
+    arr = _instances(instances)
+    res = np.zeros((n, ADJOINT_STRIDE))
+    secs = ctypes.c_double(0)
+    _check(lib().sqbem_adjoint_batch(n, ctypes.cast(arr, _VP), precision, _dp(res), ctypes.byref(secs)))
+    r = res.reshape(n, 2, 24)
+    out = dict(U=r[:, :, 0:3].copy(), Om=r[:, :, 3:6].copy(), dU_dc=r[:, :, 6:15].reshape(n, 2, 3, 3).copy(),
+               dOm_dc=r[:, :, 15:24].reshape(n, 2, 3, 3).copy())
+    return out, secs.value
 
 
 # ---------------------------------------------------------------- meshes
@@ -413,6 +438,19 @@ class SwimmerSolver:
         _check(lib().sqbem_swimmer_solve_prescribed(self._h, _dp(_f64(U)), _dp(_f64(Om)), _dp(fs),
                                                     _dp(ft) if self.Nt else None))
         return SwimmerSolution(_f64(U).copy(), _f64(Om).copy(), fs, ft)
+
+    def adjoint(self, slips):
+        """solve_free plus the derivatives of U and Omega with respect to a rigid
+        translation of the sphere: returns U (nr, 3), Om (nr, 3), dU_dc
+        (nr, 3, 3) and dOm_dc (nr, 3, 3), [k, a, j] = d(.)_a / dc_j."""
+        nr = len(slips)
+        sl = _f64(np.stack([np.asarray(s, float).reshape(-1, 3) for s in slips]))
+        U = np.zeros((nr, 3))
+        Om = np.zeros((nr, 3))
+        dU = np.zeros((nr, 3, 3))
+        dOm = np.zeros((nr, 3, 3))
+        _check(lib().sqbem_swimmer_adjoint(self._h, nr, _dp(sl), _dp(U), _dp(Om), _dp(dU), _dp(dOm)))
+        return U, Om, dU, dOm
 
     def refinement(self):
         it, res = ctypes.c_int(0), ctypes.c_double(0)
