@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="sweep", choices=["sweep", "kinematics"])
+    ap.add_argument("--instances", type=int, default=0,
+                    help="first N instances of the workload only (small cases for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -145,21 +147,36 @@ def load_peaks():
 FP64_PEAK_TFLOPS = 1.0
 
 
-def traffic_of(cls):
-    """DRAM bytes per launch of a kernel class from the committed ncu summary."""
+def traffic_of(cls, launches, flops):
+    """DRAM bytes per launch of a kernel class from the committed ncu summary:
+    'cls dram_bytes_per_flop X' (measured on a smaller capture, scaled by the
+    algorithmic flops per launch here) or 'cls dram_bytes_per_launch X'."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
-    if not os.path.exists(p):
+    if not os.path.exists(p) or launches <= 0:
         return None
     for line in open(p):
         f = line.split()
-        if len(f) >= 2 and f[0] == cls and not line.startswith("#"):
-            return float(f[1])
+        if line.startswith("#") or len(f) < 3 or f[0] != cls:
+            continue
+        if f[1] == "dram_bytes_per_flop":
+            return float(f[2]) * flops / launches
+        if f[1] == "dram_bytes_per_launch":
+            return float(f[2])
     return None
 
 
-def workload(name):
+def workload(name, n=0):
     from sqbem import workloads
-    return workloads.sweep() if name == "sweep" else workloads.kinematics()
+    w = workloads.sweep() if name == "sweep" else workloads.kinematics()
+    return w[:n] if n > 0 else w
+
+
+def config_of(args, insts, ws):
+    """the workload description shared by both arms"""
+    return {"workload": "%s (%d instances)" % (args.workload, len(insts)), "instances_per_step": len(insts),
+            "precision": args.precision, "n_theta": 24, "L_over_R": 4,
+            "l2": "per-instance working set > L2, no flush",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
 
 
 def cpu_solve(orc, inst):
@@ -198,15 +215,14 @@ def cpu_sample(insts, budget_s=20.0):
 def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
-    insts = workload(args.workload)
+    insts = workload(args.workload, args.instances)
     cores = os.cpu_count()
     # each step: one instance of the workload (cycling), the oracle on all cores
-    for _ in range(args.warmup):
-        pass  # the CPU path has no compile/warm-up state worth excluding beyond the first solve
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     orc.lib()
-    cpu_solve(orc, insts[0])  # one untimed solve
+    for k in range(max(args.warmup, 1)):  # untimed
+        cpu_solve(orc, insts[k % len(insts)])
     t0 = time.perf_counter()
     n = 0
     for k in range(args.steps):
@@ -217,7 +233,7 @@ def run_reference(args, rank, ws, dist):
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "instances_per_step": 1, "precision": "fp64 (CPU)"},
+            "config": config_of(args, insts, ws),
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
                              "sample": "%d instances of the %s workload, one per step (oracle: C assembly "
@@ -235,7 +251,7 @@ def main():
         return
     import sqbem
     prec = sqbem.MIXED if args.precision == "mixed" else sqbem.FP64
-    insts = workload(args.workload)
+    insts = workload(args.workload, args.instances)
     peaks = load_peaks()
     for _ in range(args.warmup):  # >= 3 for a valid bench line
         sqbem.kinematics_batch(insts, prec)
@@ -273,7 +289,7 @@ def main():
         else:
             achieved, peak, unit, bound = by / secs / 1e9, peaks["hbm_gbs"], "GB/s", "hbm"
         roofline = {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                    "frac": achieved / peak, "traffic": traffic_of(top), "launches": nl,
+                    "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
                     "share_of_gpu_time": secs / gpu_s if gpu_s > 0 else None,
                     "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe"}
     cpu = None
@@ -289,16 +305,15 @@ def main():
         "warmup": args.warmup, "ms_per_step": 1e3 * gpu_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32/bf16x3+f64" if prec == sqbem.MIXED else "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "instances_per_step": len(insts), "precision": args.precision,
-                   "n_theta": 24, "L_over_R": 4, "l2": "per-instance working set > L2, no flush",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": config_of(args, insts, ws),
         "e2e": {"value": solves / wall, "unit": "solves/s", "h2d_bytes_per_step": (h2d - h2d0) / args.steps,
                 "d2h_bytes_per_step": (d2h - d2h0) / args.steps},
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
         "cpu_baseline": cpu,
-        "kernel_seconds": {c: v[1] for c, v in stats.items()},
+        "kernel_stats": {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]}
+                         for c, v in stats.items()},
     }
     print(json.dumps(line), flush=True)
 

@@ -3,7 +3,9 @@ the sphere-tube kernel derivatives, against central finite differences (step
 1e-4, FP64) of the GPU solver and of the oracle, with detection of quadrature
 rule changes between the two FD positions (kernels.hpp:74-75 picks the rule by
 distance, so a step that moves a pair across d = 3, 1.5 or 0.75 makes a jump
-that is not part of the derivative; such samples are reported and skipped)."""
+that is not part of the derivative): where the nominal centre has such a
+crossing, the comparison moves to the nearest rule-clean centre and the nominal
+FD error is printed for the record."""
 import numpy as np
 import pytest
 
@@ -29,6 +31,18 @@ def rule_change(tube_mesh, level, a, c, axis):
         S = sqbem.icosphere(a, level, cc)
         out.append((rules(tube_mesh.centroid, S), rules(S.centroid, tube_mesh)))
     return not (np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]))
+
+
+def clean_point(tube_mesh, level, c, a=1.0):
+    """c itself if no FD axis straddles a rule change there, else the first of a
+    fixed sequence of nearby points (steps of 1e-3) where none does; returns the
+    point and whether it moved"""
+    d = np.array([0.31, 0.57, 0.83])
+    for k in range(40):
+        cc = np.array(c, float) + 1e-3 * k * d
+        if not any(rule_change(tube_mesh, level, a, cc, j) for j in range(3)):
+            return cc, k > 0
+    raise AssertionError("no rule-clean FD point near %s" % (c,))
 
 
 def gpu_solve(tube, level, c, e, a=1.0):
@@ -73,13 +87,14 @@ def test_adjoint_matches_gpu_fd_small():
     c = np.array([beta * (R - 1.0), 0.13, 0.21])
     e = np.array([0.3, -0.2, 0.9])
     e /= np.linalg.norm(e)
-    out, Ja = adjoint_jacobian(tube, 1, c, e)
+    out, _ = adjoint_jacobian(tube, 1, c, e)
     np.testing.assert_allclose(out, gpu_solve(tube, 1, c, e), rtol=0, atol=1e-13)
+    c, moved = clean_point(tube.mesh, 1, c)
+    _, Ja = adjoint_jacobian(tube, 1, c, e)
     Jf = fd_jacobian(lambda cc: gpu_solve(tube, 1, cc, e), c)
-    flagged = [rule_change(tube.mesh, 1, 1.0, c, j) for j in range(3)]
-    err, keep = compare(Ja, Jf, flagged)
-    print("axes", keep, "rel err", err)
-    assert err < TOL, (err, flagged)
+    err, _ = compare(Ja, Jf, [False] * 3)
+    print("moved", moved, "rel err", err)
+    assert err < TOL, err
 
 
 def test_adjoint_matches_oracle_fd(oracle):
@@ -97,35 +112,49 @@ def test_adjoint_matches_oracle_fd(oracle):
         k = s.solve_free([s.slip(e, 1, 0), s.slip(e, 0, 1)])
         return np.array([np.concatenate([k[m].U, k[m].Om]) for m in range(2)])
 
-    out, Ja = adjoint_jacobian(tube, 1, c, e)
+    out, _ = adjoint_jacobian(tube, 1, c, e)
     np.testing.assert_allclose(out, osolve(c), rtol=0, atol=1e-10 * np.max(np.abs(out)))
+    c, moved = clean_point(tube.mesh, 1, c)
+    _, Ja = adjoint_jacobian(tube, 1, c, e)
     Jf = fd_jacobian(osolve, c)
-    flagged = [rule_change(tube.mesh, 1, 1.0, c, j) for j in range(3)]
-    err, keep = compare(Ja, Jf, flagged)
-    print("axes", keep, "rel err", err)
-    assert err < TOL, (err, flagged)
+    err, _ = compare(Ja, Jf, [False] * 3)
+    print("moved", moved, "rel err", err)
+    assert err < TOL, err
 
 
 def test_adjoint_batch_config_instances():
-    """four instances of the 32-instance adjoint workload (level 2, n_theta = 24)"""
+    """the 32-instance adjoint workload (a/R ~ U[0.2, 0.5], beta ~ U[0, 0.5],
+    level 2, n_theta = 24): batch output = single-instance adjoint at the nominal
+    centre; adjoint vs central FD at the nominal centre where no FD step changes
+    a quadrature rule, else at the nearest rule-clean point"""
     from sqbem import workloads
-    inst = workloads.adjoint()[:4]
+    inst = workloads.adjoint()
     res, secs = sqbem.adjoint_batch(inst)
     assert secs > 0
+    worst, moved_n = 0.0, 0
     for k, d in enumerate(inst):
         R = 1.0 / d["a_over_R"]
         tube = sqbem.Tube(R, d["L_over_R"] * R, 1.0, d["n_theta"], d["n_r"])
         c = np.array([d["beta"] * (R - 1.0), 0.0, 0.0])
         e = np.array(d["e"])
-        out = np.concatenate([res["U"][k], res["Om"][k]], axis=1)
+        out, Jn = adjoint_jacobian(tube, 2, c, e)
+        np.testing.assert_array_equal(np.concatenate([res["U"][k], res["Om"][k]], axis=1), out)
+        np.testing.assert_array_equal(np.concatenate([res["dU_dc"][k], res["dOm_dc"][k]], axis=1), Jn)
         np.testing.assert_allclose(out, gpu_solve(tube, 2, c, e), rtol=0, atol=1e-12)
-        Ja = np.concatenate([res["dU_dc"][k], res["dOm_dc"][k]], axis=1)
-        Jf = fd_jacobian(lambda cc: gpu_solve(tube, 2, cc, e), c)
-        flagged = [rule_change(tube.mesh, 2, 1.0, c, j) for j in range(3)]
-        err, keep = compare(Ja, Jf, flagged)
-        print("instance", k, "axes", keep, "rel err", err)
-        assert err < TOL, (k, err, flagged)
+        cc, moved = clean_point(tube.mesh, 2, c)
+        moved_n += moved
+        if moved:
+            Jfn = fd_jacobian(lambda x: gpu_solve(tube, 2, x, e), c)
+            print("instance", k, "nominal centre straddles a rule change: FD rel err there",
+                  compare(Jn, Jfn, [False] * 3)[0])
+        Ja = Jn if not moved else adjoint_jacobian(tube, 2, cc, e)[1]
+        Jf = fd_jacobian(lambda x: gpu_solve(tube, 2, x, e), cc)
+        err, _ = compare(Ja, Jf, [False] * 3)
+        worst = max(worst, err)
+        print("instance", k, "moved", moved, "rel err", err)
+        assert err < TOL, (k, err)
         tube.close()
+    print("32 instances: worst rel err %.3e, %d moved to a rule-clean point" % (worst, moved_n))
 
 
 def test_B2_derivative_is_linear_mode():
@@ -167,7 +196,8 @@ def test_autograd_function_backward():
     from sqbem.autograd import kinematics
     R = 1.0 / 0.3
     tube = sqbem.Tube(R, 4 * R, 1.0, 12)
-    c = torch.tensor([0.6, 0.1, -0.2], dtype=torch.float64, requires_grad=True)
+    c0, _ = clean_point(tube.mesh, 1, np.array([0.6, 0.1, -0.2]))
+    c = torch.tensor(c0, dtype=torch.float64, requires_grad=True)
     alpha = torch.tensor(2.0, dtype=torch.float64, requires_grad=True)
     e = (0.0, 0.0, 1.0)
     U, Om = kinematics(tube, c, alpha, e, level=1)
@@ -176,20 +206,16 @@ def test_autograd_function_backward():
     (U @ w + Om @ v).backward()
 
     def J(cc, al):
-        u, o = kinematics(tube, torch.tensor(cc), torch.tensor(al), e, level=1)
+        u, o = kinematics(tube, torch.tensor(cc, dtype=torch.float64), torch.tensor(al, dtype=torch.float64), e,
+                          level=1)
         return float(u @ w + o @ v)
 
-    c0 = c.detach().numpy()
     g = np.zeros(3)
     for j in range(3):
         cp, cm = c0.copy(), c0.copy()
         cp[j] += H
         cm[j] -= H
         g[j] = (J(cp, 2.0) - J(cm, 2.0)) / (2 * H)
-    flagged = [rule_change(tube.mesh, 1, 1.0, c0, j) for j in range(3)]
-    keep = [j for j in range(3) if not flagged[j]]
-    assert keep
-    scale = np.max(np.abs(g))
-    assert np.max(np.abs(c.grad.numpy()[keep] - g[keep])) < TOL * scale
-    ga = (J(c0, 2.0 + H) - J(c0, 2.0 - H)) / (2 * H)
+    assert np.max(np.abs(c.grad.numpy() - g)) < TOL * np.max(np.abs(g))
+    ga = (J(c0, 2.0 + H) - J(c0, 2.0 - H)) / (2 * H)  # exact up to rounding: U is linear in alpha
     assert abs(float(alpha.grad) - ga) < 1e-8 * max(1.0, abs(ga))
