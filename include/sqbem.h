@@ -264,6 +264,19 @@ int sqbem_trajectory_ensemble(int n, const double* y0, const double* alpha, cons
                               int steps, int scheme, int precision, double* states, double* U, double* Om,
                               int* status, double* device_seconds);
 
+/* Velocity field of n swimmers (the field mode of src/main.cpp:109-150 over a
+ * 3-D grid, per swimmer, for an ensemble): swimmer k at states[6k..] = (x, y,
+ * z, ex, ey, ez) with B1 = 1, B2 = alpha[k], in the tube of *p (centred on the
+ * swimmer, so z is not used).  Grid: x_i = -0.97 R + 1.94 R i / (nx - 1), y_j
+ * likewise, z_l = -z_extent + 2 z_extent l / (nz - 1); the lab-frame velocity
+ * (swimmer.hpp:163-173) goes to u[(((k nx + i) ny + j) nz + l) * 3 ..], NaN at
+ * points outside r = 0.97 R or within 1.03 a of the sphere centre.  Mixed
+ * precision evaluates the 7-point rule in FP32 and the near panels (d < 3) in
+ * FP32 / FP64 (448-point rule); FP64 everywhere otherwise. */
+int sqbem_ensemble_field(int n, const double* states, const double* alpha, const sqbem_traj_params* p,
+                         int nx, int ny, int nz, double z_extent, int precision, double* u,
+                         double* device_seconds);
+
 #ifdef __cplusplus
 }
 #endif

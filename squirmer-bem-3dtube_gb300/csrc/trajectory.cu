@@ -10,6 +10,7 @@
 // refinement), with the tube's inverse shared by all of them.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -32,6 +33,22 @@ using State = std::array<double, 6>;  // x, y, z, ex, ey, ez
 
 constexpr int TRAJ_GROUP = 48;
 
+// Field grid of one swimmer (the y = 0 plane of the reference's field mode,
+// main.cpp:109-131, extended to 3-D): x, y in [-0.97 R, 0.97 R], z in
+// [-z_extent, z_extent] around the sphere (the tube frame is centred on the
+// swimmer); points outside r = 0.97 R or within 1.03 a of the centre are masked.
+struct GridSpec {
+    int nx = 25, ny = 25, nz = 41;
+    double z_extent = 7.0;
+};
+
+// out[i] = x[i] + alpha x[ld + i]: the B1 + alpha B2 combination of two solutions
+__global__ void combine_modes_kernel(const double* __restrict__ x, long long ld, int n, double alpha,
+                                     double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = x[i] + alpha * x[ld + i];
+}
+
 struct Modes {
     double U1[3], O1[3], U2[3], O2[3];
 };
@@ -50,79 +67,117 @@ public:
     double a() const { return a_; }
     cudaStream_t stream() const { return tube_->st; }
 
+    // One group of swimmers built and solved for the B1 and B2 slip modes.  With
+    // keep, the full solutions stay available: mixed, x = [f_t; f_s; w] per mode
+    // on the device (ld = nt + nc); FP64, f_t and f_s per mode on the host.
+    struct Group {
+        std::vector<std::unique_ptr<sqbem_swimmer>> sw;
+        std::vector<std::vector<double>> slips;  // 2 x 3 Ns per swimmer
+        std::vector<Modes> modes;
+        std::vector<DevBuf<double>> dx;          // mixed
+        std::vector<std::vector<double>> ft, fs; // FP64: 2 x 3 Nt, 2 x 3 Ns
+        std::vector<std::array<double, 3>> centre;
+    };
+
+    void solve_group(const std::vector<State>& ys, size_t c0, size_t G, bool keep, Group& gr) {
+        gr.sw.resize(G);
+        gr.slips.resize(G);
+        gr.modes.resize(G);
+        gr.centre.resize(G);
+        for (size_t g = 0; g < G; ++g) {
+            const State& y = ys[c0 + g];
+            const double c[3] = {y[0], y[1], 0.0};
+            gr.centre[g] = {c[0], c[1], c[2]};
+            bem::Mesh S = sph0_;
+            S.translate({c[0], c[1], c[2]});
+            const auto V = mesh_vertices(S);
+            gr.sw[g] = std::make_unique<sqbem_swimmer>();
+            gr.sw[g]->st.borrow(tube_->st);
+            const bem::V3 e = bem::unit(bem::V3{y[3], y[4], y[5]});
+            const double ev[3] = {e.x, e.y, e.z};
+            if (prec_ == SQBEM_MIXED) {
+                gr.sw[g]->set_geometry(tube_.get(), S.P(), V.data(), c, 1.0, prec_);
+            } else {
+                gr.sw[g]->build(tube_.get(), S.P(), V.data(), c, 1.0, prec_);
+            }
+            gr.slips[g] = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 1, 0);
+            const auto u2 = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 0, 1);
+            gr.slips[g].insert(gr.slips[g].end(), u2.begin(), u2.end());
+        }
+        if (prec_ == SQBEM_MIXED) {
+            std::vector<sqbem_swimmer*> sp;
+            for (auto& s : gr.sw) sp.push_back(s.get());
+            DevBuf<int> flags(2, tube_->st);
+            flags.zero();
+            MixedCtx cx{tube_->st, flags.get(), flags.get() + 1};
+            mixed_build_swimmers(sp, cx);
+            std::vector<DevBuf<double>> din(G);
+            gr.dx.clear();
+            gr.dx.resize(G);
+            std::vector<const double*> ip;
+            std::vector<double*> xp;
+            for (size_t g = 0; g < G; ++g) {
+                din[g].alloc(gr.slips[g].size(), tube_->st);
+                din[g].upload(gr.slips[g].data(), gr.slips[g].size());
+                gr.dx[g].alloc((size_t)(sp[g]->mx.nt + sp[g]->mx.nc) * 2, tube_->st);
+                ip.push_back(din[g].get());
+                xp.push_back(gr.dx[g].get());
+            }
+            int it = 0;
+            double res = 0;
+            mixed_solve(sp, false, ip, 2, xp, cx, &it, &res);
+            for (size_t g = 0; g < G; ++g) {
+                const MixedSwimmer& M = sp[g]->mx;
+                const size_t ld = (size_t)M.nt + M.nc;
+                std::vector<double> w(12);
+                for (int k = 0; k < 2; ++k)
+                    CUDA_CHECK(cudaMemcpyAsync(w.data() + 6 * k, gr.dx[g].get() + k * ld + M.nt + M.ns,
+                                               6 * sizeof(double), cudaMemcpyDeviceToHost, tube_->st));
+                count_d2h(12 * sizeof(double));
+                CUDA_CHECK(cudaStreamSynchronize(tube_->st));
+                Modes& m = gr.modes[g];
+                for (int q = 0; q < 3; ++q) {
+                    m.U1[q] = w[q]; m.O1[q] = w[3 + q]; m.U2[q] = w[6 + q]; m.O2[q] = w[9 + q];
+                }
+            }
+            if (!keep) gr.dx.clear();
+        } else {
+            if (keep) {
+                gr.ft.resize(G);
+                gr.fs.resize(G);
+            }
+            for (size_t g = 0; g < G; ++g) {
+                double U[6], Om[6];
+                sqbem_swimmer& s = *gr.sw[g];
+                if (keep) {
+                    gr.ft[g].resize((size_t)6 * s.Nt);
+                    gr.fs[g].resize((size_t)6 * s.Ns);
+                }
+                s.solve_free(2, gr.slips[g].data(), U, Om, keep ? gr.fs[g].data() : nullptr,
+                             keep ? gr.ft[g].data() : nullptr);
+                Modes& m = gr.modes[g];
+                for (int q = 0; q < 3; ++q) {
+                    m.U1[q] = U[q]; m.O1[q] = Om[q]; m.U2[q] = U[3 + q]; m.O2[q] = Om[3 + q];
+                }
+            }
+        }
+        evals_ += G;
+    }
+
     std::vector<Modes> modes(const std::vector<State>& ys) {
         std::vector<Modes> out(ys.size());
         for (size_t c0 = 0; c0 < ys.size(); c0 += TRAJ_GROUP) {
             const size_t G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
-            std::vector<std::unique_ptr<sqbem_swimmer>> sw(G);
-            std::vector<std::vector<double>> slips(G);
-            for (size_t g = 0; g < G; ++g) {
-                const State& y = ys[c0 + g];
-                const double c[3] = {y[0], y[1], 0.0};
-                bem::Mesh S = sph0_;
-                S.translate({c[0], c[1], c[2]});
-                const auto V = mesh_vertices(S);
-                sw[g] = std::make_unique<sqbem_swimmer>();
-                sw[g]->st.borrow(tube_->st);
-                const bem::V3 e = bem::unit(bem::V3{y[3], y[4], y[5]});
-                const double ev[3] = {e.x, e.y, e.z};
-                if (prec_ == SQBEM_MIXED) {
-                    sw[g]->set_geometry(tube_.get(), S.P(), V.data(), c, 1.0, prec_);
-                } else {
-                    sw[g]->build(tube_.get(), S.P(), V.data(), c, 1.0, prec_);
-                }
-                slips[g] = squirmer_slip_host(sw[g]->host_panels, c, ev, 1, 0);
-                const auto u2 = squirmer_slip_host(sw[g]->host_panels, c, ev, 0, 1);
-                slips[g].insert(slips[g].end(), u2.begin(), u2.end());
-            }
-            if (prec_ == SQBEM_MIXED) {
-                std::vector<sqbem_swimmer*> sp;
-                for (auto& s : sw) sp.push_back(s.get());
-                DevBuf<int> flags(2, tube_->st);
-                flags.zero();
-                MixedCtx cx{tube_->st, flags.get(), flags.get() + 1};
-                mixed_build_swimmers(sp, cx);
-                std::vector<DevBuf<double>> din(G), dx(G);
-                std::vector<const double*> ip;
-                std::vector<double*> xp;
-                for (size_t g = 0; g < G; ++g) {
-                    din[g].alloc(slips[g].size(), tube_->st);
-                    din[g].upload(slips[g].data(), slips[g].size());
-                    dx[g].alloc((size_t)(sp[g]->mx.nt + sp[g]->mx.nc) * 2, tube_->st);
-                    ip.push_back(din[g].get());
-                    xp.push_back(dx[g].get());
-                }
-                int it = 0;
-                double res = 0;
-                mixed_solve(sp, false, ip, 2, xp, cx, &it, &res);
-                for (size_t g = 0; g < G; ++g) {
-                    const MixedSwimmer& M = sp[g]->mx;
-                    const size_t ld = (size_t)M.nt + M.nc;
-                    std::vector<double> w(12);
-                    for (int k = 0; k < 2; ++k)
-                        CUDA_CHECK(cudaMemcpyAsync(w.data() + 6 * k, dx[g].get() + k * ld + M.nt + M.ns, 6 * sizeof(double),
-                                                   cudaMemcpyDeviceToHost, tube_->st));
-                    count_d2h(12 * sizeof(double));
-                    CUDA_CHECK(cudaStreamSynchronize(tube_->st));
-                    Modes& m = out[c0 + g];
-                    for (int q = 0; q < 3; ++q) {
-                        m.U1[q] = w[q]; m.O1[q] = w[3 + q]; m.U2[q] = w[6 + q]; m.O2[q] = w[9 + q];
-                    }
-                }
-            } else {
-                for (size_t g = 0; g < G; ++g) {
-                    double U[6], Om[6];
-                    sw[g]->solve_free(2, slips[g].data(), U, Om, nullptr, nullptr);
-                    Modes& m = out[c0 + g];
-                    for (int q = 0; q < 3; ++q) {
-                        m.U1[q] = U[q]; m.O1[q] = Om[q]; m.U2[q] = U[3 + q]; m.O2[q] = Om[3 + q];
-                    }
-                }
-            }
-            evals_ += G;
+            Group gr;
+            solve_group(ys, c0, G, false, gr);
+            for (size_t g = 0; g < G; ++g) out[c0 + g] = gr.modes[g];
         }
         return out;
     }
+
+    // Lab-frame velocity (swimmer.hpp:163-173, field.hpp:18-34) of swimmer k
+    // (B1 = 1, B2 = alpha[k]) at the unmasked points of its grid.
+    void fields(const std::vector<State>& ys, const double* alpha, const GridSpec& gs, double* u_out);
     long long evals() const { return evals_; }
 
 private:
@@ -132,6 +187,104 @@ private:
     bem::Mesh sph0_;
     long long evals_ = 0;
 };
+
+void Evaluator::fields(const std::vector<State>& ys, const double* alpha, const GridSpec& gs, double* u_out) {
+    const int Nt = tube_->Nt;
+    const size_t npg = (size_t)gs.nx * gs.ny * gs.nz;
+    const double lim = 0.97 * R_;
+    cudaStream_t st = tube_->st;
+    for (size_t c0 = 0; c0 < ys.size(); c0 += TRAJ_GROUP) {
+        const size_t G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
+        Group gr;
+        solve_group(ys, c0, G, true, gr);
+        for (size_t g = 0; g < G; ++g) {
+            const size_t k = c0 + g;
+            sqbem_swimmer& s = *gr.sw[g];
+            const int Ns = s.Ns, P = Nt + Ns;
+            const double al = alpha[k];
+            const std::array<double, 3>& c = gr.centre[g];
+            double* uk = u_out + k * npg * 3;
+            std::vector<double> pts;
+            std::vector<size_t> idx;
+            for (int i = 0; i < gs.nx; ++i)
+                for (int j = 0; j < gs.ny; ++j)
+                    for (int l = 0; l < gs.nz; ++l) {
+                        const size_t q = ((size_t)i * gs.ny + j) * gs.nz + l;
+                        const double x = -lim + 2 * lim * i / (gs.nx - 1), y = -lim + 2 * lim * j / (gs.ny - 1);
+                        const double z = -gs.z_extent + 2 * gs.z_extent * l / (gs.nz - 1);
+                        const double dx = x - c[0], dy = y - c[1], dz = z - c[2];
+                        uk[3 * q] = uk[3 * q + 1] = uk[3 * q + 2] = NAN;
+                        if (x * x + y * y > lim * lim || std::sqrt(dx * dx + dy * dy + dz * dz) < 1.03 * a_) continue;
+                        pts.insert(pts.end(), {x, y, z});
+                        idx.push_back(q);
+                    }
+            if (idx.empty()) continue;
+            const int npts = (int)idx.size();
+            DevBuf<PanelRec> mp((size_t)P, st);
+            CUDA_CHECK(cudaMemcpyAsync(mp.get(), tube_->panels.rec.get(), sizeof(PanelRec) * Nt,
+                                       cudaMemcpyDeviceToDevice, st));
+            CUDA_CHECK(cudaMemcpyAsync(mp.get() + Nt, s.panels.rec.get(), sizeof(PanelRec) * Ns,
+                                       cudaMemcpyDeviceToDevice, st));
+            // tractions f = f[B1] + alpha f[B2], tube panels first (the order of x)
+            DevBuf<double> df(3 * (size_t)P, st);
+            if (prec_ == SQBEM_MIXED) {
+                const long long ld = (long long)s.mx.nt + s.mx.nc;
+                LAUNCH(combine_modes_kernel, ceil_div(3LL * P, 256), 256, 0, st, gr.dx[g].get(), ld, 3 * P, al,
+                       df.get());
+            } else {
+                std::vector<double> hf(3 * (size_t)P);
+                for (int i = 0; i < 3 * Nt; ++i) hf[i] = gr.ft[g][i] + al * gr.ft[g][3 * (size_t)Nt + i];
+                for (int i = 0; i < 3 * Ns; ++i) hf[3 * (size_t)Nt + i] = gr.fs[g][i] + al * gr.fs[g][3 * (size_t)Ns + i];
+                df.upload(hf.data(), hf.size());
+            }
+            // surface velocity: 0 on the tube, U + Omega x r + slip on the sphere
+            const Modes& m = gr.modes[g];
+            double U[3], W[3];
+            for (int q = 0; q < 3; ++q) {
+                U[q] = m.U1[q] + al * m.U2[q];
+                W[q] = m.O1[q] + al * m.O2[q];
+            }
+            std::vector<double> hu(3 * (size_t)P, 0.0);
+            const std::vector<double>& sl = gr.slips[g];
+            for (int p = 0; p < Ns; ++p) {
+                const double rx = s.host_panels[p].c[0] - c[0], ry = s.host_panels[p].c[1] - c[1],
+                             rz = s.host_panels[p].c[2] - c[2];
+                double* o = hu.data() + 3 * ((size_t)Nt + p);
+                const double* s1 = sl.data() + 3 * p;
+                const double* s2 = sl.data() + 3 * ((size_t)Ns + p);
+                o[0] = U[0] + (W[1] * rz - W[2] * ry) + (s1[0] + al * s2[0]);
+                o[1] = U[1] + (W[2] * rx - W[0] * rz) + (s1[1] + al * s2[1]);
+                o[2] = U[2] + (W[0] * ry - W[1] * rx) + (s1[2] + al * s2[2]);
+            }
+            DevBuf<double> du(hu.size(), st), dpts(pts.size(), st), dout(pts.size(), st);
+            DevBuf<int> ovf(1, st);
+            ovf.zero();
+            du.upload(hu.data(), hu.size());
+            dpts.upload(pts.data(), pts.size());
+            FieldJob job;
+            job.pts = dpts.get();
+            job.npts = npts;
+            job.panels = mp.get();
+            job.P = P;
+            job.u = du.get();
+            job.f = df.get();
+            job.sscale = 1.0 / EIGHT_PI;  // mu = 1
+            job.dscale = -1.0 / EIGHT_PI;
+            job.out = dout.get();
+            job.overflow = ovf.get();
+            job.mixed = prec_ == SQBEM_MIXED;
+            field_eval(job, st);
+            std::vector<double> ho(pts.size());
+            int h_ovf = 0;
+            dout.download(ho.data(), ho.size());
+            ovf.download(&h_ovf, 1);
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            if (h_ovf) fail(SQBEM_ERR_ARG, "ensemble_field: a grid point has more than 256 near panels");
+            for (int q = 0; q < npts; ++q)
+                for (int d = 0; d < 3; ++d) uk[3 * idx[q] + d] = ho[3 * (size_t)q + d];
+        }
+    }
+}
 
 // state derivative (trajectory.hpp:52-65): U = U1 + alpha U2, de/dt = Omega x e
 State derivative(const State& y, const Modes& m, double alpha, double* U, double* Om) {
@@ -374,6 +527,38 @@ extern "C" int sqbem_trajectory_ensemble(int n, const double* y0, const double* 
                     if (Om) Om[((size_t)ids[j] * steps + s) * 3 + i] = uo[j][3 + i];
                 }
         }
+        clk.stop(ev.stream());
+        const double secs = clk.seconds();
+        if (device_seconds) *device_seconds = secs;
+    });
+}
+
+extern "C" int sqbem_ensemble_field(int n, const double* states, const double* alpha, const sqbem_traj_params* pp,
+                                    int nx, int ny, int nz, double z_extent, int precision, double* u,
+                                    double* device_seconds) {
+    return guarded([&] {
+        if (n < 0 || !pp || nx < 2 || ny < 2 || nz < 2 || !(z_extent > 0) || (n > 0 && (!states || !alpha || !u)) ||
+            (precision != SQBEM_FP64 && precision != SQBEM_MIXED))
+            fail(SQBEM_ERR_ARG, "ensemble_field: bad arguments");
+        const sqbem_traj_params P = *pp;
+        check_params(P);
+        if (device_seconds) *device_seconds = 0;
+        if (n == 0) return;
+        require_device();
+        Evaluator ev(P, precision);
+        std::vector<State> ys(n);
+        for (int k = 0; k < n; ++k) {
+            for (int i = 0; i < 6; ++i) ys[k][i] = states[6 * k + i];
+            normalise_e(ys[k]);
+        }
+        GridSpec gs;
+        gs.nx = nx;
+        gs.ny = ny;
+        gs.nz = nz;
+        gs.z_extent = z_extent;
+        EventTimer clk;
+        clk.start(ev.stream());
+        ev.fields(ys, alpha, gs, u);
         clk.stop(ev.stream());
         const double secs = clk.seconds();
         if (device_seconds) *device_seconds = secs;

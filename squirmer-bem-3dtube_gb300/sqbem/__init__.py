@@ -77,6 +77,7 @@ SIGNATURES = {
     "sqbem_trajectory_defaults": (_c_i, [_VP]),
     "sqbem_run_trajectory": (_c_i, [_VP, ctypes.c_char_p, _c_i, _c_i, ctypes.c_char_p, _c_i]),
     "sqbem_trajectory_ensemble": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _D, _D, _D, _I, _D]),
+    "sqbem_ensemble_field": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _c_d, _c_i, _D, _D]),
     "sqbem_gemm_mixed": (_c_i, [_c_i, _c_i, _c_i, ctypes.c_float, ctypes.POINTER(ctypes.c_float), _c_i,
                                 ctypes.POINTER(ctypes.c_float), _c_i, ctypes.c_float,
                                 ctypes.POINTER(ctypes.c_float), _c_i]),
@@ -134,6 +135,33 @@ def trajectory_ensemble(y0, alpha, P, steps, scheme=1, precision=MIXED):
     _check(lib().sqbem_trajectory_ensemble(n, _dp(y0), _dp(al), ctypes.byref(P), steps, scheme, precision,
                                            _dp(states), _dp(U), _dp(Om), _ip(status), ctypes.byref(secs)))
     return states, U, Om, status, secs.value
+
+
+def ensemble_field(states, alpha, P, nx=25, ny=25, nz=41, z_extent=7.0, precision=MIXED):
+    """Velocity on an nx x ny x nz grid per swimmer (x, y in [-0.97 R, 0.97 R],
+    z in [-z_extent, z_extent] around the sphere; NaN outside the tube section and
+    within 1.03 a of the centre).  Returns (u (n, nx, ny, nz, 3), device seconds)."""
+    st = _f64(states).reshape(-1, 6)
+    n = st.shape[0]
+    al = _f64(np.broadcast_to(np.asarray(alpha, dtype=np.float64), (n,)))
+    u = np.zeros((n, nx, ny, nz, 3))
+    secs = ctypes.c_double(0)
+    _check(lib().sqbem_ensemble_field(n, _dp(st), _dp(al), ctypes.byref(P), nx, ny, nz, z_extent, precision, _dp(u),
+                                      ctypes.byref(secs)))
+    return u, secs.value
+
+
+def field_grid(R, c, nx=25, ny=25, nz=41, z_extent=7.0, a=1.0):
+    """The points of ensemble_field's grid (n, 3) and its mask (True = evaluated)."""
+    lim = 0.97 * R
+    x = -lim + 2 * lim * np.arange(nx) / (nx - 1)
+    y = -lim + 2 * lim * np.arange(ny) / (ny - 1)
+    z = -z_extent + 2 * z_extent * np.arange(nz) / (nz - 1)
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    pts = np.stack([X, Y, Z], axis=-1).reshape(-1, 3)
+    d = np.sqrt(np.sum((pts - np.asarray(c, float)[None, :]) ** 2, axis=1))
+    mask = (pts[:, 0] ** 2 + pts[:, 1] ** 2 <= lim * lim) & (d >= 1.03 * a)
+    return pts, mask
 
 
 class Instance(ctypes.Structure):

@@ -143,3 +143,69 @@ def test_ensemble_wall_contact_freezes_member():
     assert status[0] == 1 and status[1] == 0
     np.testing.assert_array_equal(states[0, 2], y0[0])
     assert np.all(np.isnan(U[0]))
+
+
+def _field_reference(P, y, alpha, pts, tube, precision=sqbem.FP64):
+    """single-swimmer API: SwimmerSolver.velocity for the combined slip"""
+    c = np.array([y[0], y[1], 0.0])
+    e = np.array(y[3:6]) / np.linalg.norm(y[3:6])
+    S = sqbem.icosphere(1.0, P.sphere_level, c)
+    s = sqbem.SwimmerSolver(tube, S, c, precision=precision)
+    slip = s.slip(e, 1.0, alpha)
+    sol = s.solve_free([slip])[0]
+    return s.velocity(sol, slip, pts)
+
+
+def test_ensemble_field_fp64_matches_swimmer_velocity():
+    P = sqbem.TrajParams(a_over_R=0.3, n_theta=10, sphere_level=1)
+    R = 1.0 / P.a_over_R
+    y = np.array([[0.5, -0.3, 2.0, 0.0, 0.6, 0.8], [-0.8, 0.2, 0.0, 1.0, 0.0, 0.0]])
+    alpha = np.array([-2.0, 3.0])
+    nx, ny, nz = 9, 8, 11
+    u, secs = sqbem.ensemble_field(y, alpha, P, nx, ny, nz, 5.0, precision=sqbem.FP64)
+    assert secs > 0 and u.shape == (2, nx, ny, nz, 3)
+    tube = sqbem.Tube(R, P.L_over_R * R, 1.0, P.n_theta, 4)
+    for k in range(2):
+        pts, mask = sqbem.field_grid(R, (y[k, 0], y[k, 1], 0.0), nx, ny, nz, 5.0)
+        uk = u[k].reshape(-1, 3)
+        assert np.all(np.isnan(uk[~mask])) and not np.any(np.isnan(uk[mask]))
+        ref = _field_reference(P, y[k], alpha[k], pts[mask], tube)
+        err = np.max(np.abs(uk[mask] - ref)) / np.max(np.abs(ref))
+        assert err < 1e-11, err
+
+
+def test_ensemble_field_matches_oracle(oracle):
+    P = sqbem.TrajParams(a_over_R=0.35, n_theta=8, sphere_level=1)
+    R = 1.0 / P.a_over_R
+    y = np.array([[0.4, 0.1, 0.0, 0.0, 0.0, 1.0]])
+    u, _ = sqbem.ensemble_field(y, [1.5], P, 5, 5, 7, 4.0, precision=sqbem.FP64)
+    pts, mask = sqbem.field_grid(R, (0.4, 0.1, 0.0), 5, 5, 7, 4.0)
+    c = np.array([0.4, 0.1, 0.0])
+    otube = oracle.Tube(R, P.L_over_R * R, 1.0, P.n_theta)
+    s = oracle.SwimmerSolver(otube, oracle.icosphere(1.0, 1, c), c)
+    slip = s.slip(np.array([0.0, 0.0, 1.0]), 1.0, 1.5)
+    sol = s.solve_free([slip])[0]
+    ref = s.velocity(sol, slip, pts[mask])
+    err = np.max(np.abs(u[0].reshape(-1, 3)[mask] - ref)) / np.max(np.abs(ref))
+    assert err < 1e-10, err
+
+
+def test_ensemble_field_mixed_vs_fp64():
+    P = sqbem.TrajParams(a_over_R=0.3, n_theta=24, sphere_level=2)
+    rng = np.random.default_rng(11)
+    R = 1.0 / P.a_over_R
+    n = 3
+    y = np.zeros((n, 6))
+    for k in range(n):
+        b = rng.uniform(0, 0.6) * (R - 1.0)
+        ph = rng.uniform(0, 2 * math.pi)
+        e = rng.normal(size=3)
+        y[k] = [b * math.cos(ph), b * math.sin(ph), 0.0, *(e / np.linalg.norm(e))]
+    alpha = rng.uniform(-5, 5, n)
+    u64, _ = sqbem.ensemble_field(y, alpha, P, 13, 13, 21, 7.0, precision=sqbem.FP64)
+    umx, t = sqbem.ensemble_field(y, alpha, P, 13, 13, 21, 7.0, precision=sqbem.MIXED)
+    ok = ~np.isnan(u64)
+    assert np.array_equal(ok, ~np.isnan(umx))
+    err = np.max(np.abs(umx[ok] - u64[ok])) / np.max(np.abs(u64[ok]))
+    print("mixed field rel err", err)
+    assert err < 2e-5, err
