@@ -165,9 +165,11 @@ def traffic_of(cls, launches, flops):
     return None
 
 
-def workload(name, n=0):
+def workload(name, n=0, rank=0):
+    """the instances rank `rank` solves: independent seeded shards, rank 0 = the
+    single-GPU workload (weak scaling: the per-GPU work is fixed)"""
     from sqbem import workloads
-    w = workloads.sweep() if name == "sweep" else workloads.kinematics()
+    w = workloads.sweep(shard=rank) if name == "sweep" else workloads.kinematics()
     return w[:n] if n > 0 else w
 
 
@@ -251,7 +253,7 @@ def main():
         return
     import sqbem
     prec = sqbem.MIXED if args.precision == "mixed" else sqbem.FP64
-    insts = workload(args.workload, args.instances)
+    insts = workload(args.workload, args.instances, rank)
     peaks = load_peaks()
     for _ in range(args.warmup):  # >= 3 for a valid bench line
         sqbem.kinematics_batch(insts, prec)

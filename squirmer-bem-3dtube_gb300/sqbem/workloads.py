@@ -27,8 +27,10 @@ def kinematics():
                  towed=1, alpha=0.0)]
 
 
-def sweep(n=128):
-    rng = np.random.default_rng(SEED + 2)
+def sweep(n=128, shard=0):
+    """shard > 0 draws another independent set of n instances (replica k of a
+    multi-GPU run); shard 0 is the benchmark set itself"""
+    rng = np.random.default_rng(SEED + 2) if shard == 0 else np.random.default_rng([SEED + 2, shard])
     lam = rng.uniform(0.1, 0.6, n)
     beta = rng.uniform(0.0, 1.0, n) * 0.8 * (1.0 - lam)
     alpha = rng.uniform(-5.0, 5.0, n)
