@@ -52,6 +52,8 @@ inline void count_d2h(size_t b) { g_d2h_bytes.fetch_add((long long)b, std::memor
 // launches of one class on their own stream, with the algorithmic flops and
 // bytes each launch is credited with.
 bool kstats_on();
+// free-form description attached to the next timed launch of this thread
+void kstat_note(const std::string& note);
 int kstat_begin(cudaStream_t st);
 void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double bytes);
 #define TIMED_LAUNCH(cls, flops, bytes, kernel, grid, block, smem, stream, ...)          \

@@ -1,12 +1,22 @@
 // matvec.cu -- grouped FP64-accumulated matrix-vector products and helpers.
 //
 // matvec: one thread per row, columns split into chunks of MV_CHUNK across
-// blockIdx.y (coalesced column-major reads, the vector broadcast); chunk partial
-// sums land in a scratch array and are added in chunk order by a second kernel,
-// so the result does not depend on scheduling.
+// blockIdx.y (coalesced column-major reads, the vector chunk staged in shared
+// memory); chunk partial sums land in a scratch array and are added in chunk
+// order by a second kernel, so the result does not depend on scheduling.
+//
+// FP32 matrices: GB300's FP64 pipe (about 1/64 of the FP32 rate) would bound an
+// FP64 multiply-add per element far below HBM speed, so the FP32 x FP64 products
+// are accumulated in FP32 pairs instead: x = xh + xl (two FP32 parts), and per
+// element the compensated dot product of Ogita, Rump and Oishi ("Dot2", SIAM J.
+// Sci. Comput. 26, 2005): TwoProduct by FMA, TwoSum of the running sum, the
+// errors and a * xl gathered in a second FP32 accumulator.  The chunk result
+// (double)s + (double)c is as accurate as a sum formed in twice the FP32
+// precision, close to FP64 for the residuals of the refinement.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 
 #include "common.cuh"
 #include "matvec.cuh"
@@ -38,6 +48,60 @@ struct NormArgs {
     int n;
     NormJob j[MAXJOBS];
 };
+
+// compensated FP32 multiply-accumulate: (s, c) += a * (xh + xl).  The error-free
+// transformations use the _rn intrinsics, which the compiler never fuses into
+// multiply-adds (a fused s + a * xh would break TwoSum's exactness).
+__device__ __forceinline__ void dot2_step(float& s, float& c, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float e = __fmaf_rn(a, xh, -p);  // exact: a * xh = p + e
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));  // exact: s + p = t + err
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, e));
+    c = __fmaf_rn(a, xl, c);
+}
+
+template <int R>
+__global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ MvArgs args,
+                                                        double* __restrict__ part) {
+    __shared__ float xs[R][2][MV_CHUNK];
+    const int jb = blockIdx.z, c = blockIdx.y;
+    const int nchunk = args.j[jb].nchunk;
+    if (c >= nchunk) return;
+    const float* __restrict__ A = args.j[jb].j.A32;
+    const double* __restrict__ X = args.j[jb].j.x;
+    const long long lda = args.j[jb].j.lda, ldx = args.j[jb].j.ldx;
+    const int m = args.j[jb].j.m, n = args.j[jb].j.n, r = args.j[jb].j.r;
+    const long long poff = args.j[jb].part_off;
+    const int rstride = args.j[jb].rstride;
+    const int j0 = c * MV_CHUNK, nj = min(n, j0 + MV_CHUNK) - j0;
+    for (int e = threadIdx.x; e < R * MV_CHUNK; e += MV_ROWS) {
+        const int k = e / MV_CHUNK, j = e % MV_CHUNK;
+        const double v = (k < r && j < nj) ? X[j0 + j + (long long)k * ldx] : 0.0;
+        const float h = (float)v;
+        xs[k][0][j] = h;
+        xs[k][1][j] = (float)(v - (double)h);
+    }
+    __syncthreads();
+    const int row = blockIdx.x * MV_ROWS + threadIdx.x;
+    if (row >= m) return;
+    float s[R], cc[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) s[k] = cc[k] = 0.f;
+    const float* a = A + row + (long long)j0 * lda;
+#pragma unroll 8
+    for (int j = 0; j < nj; ++j, a += lda) {
+        const float v = __ldg(a);
+#pragma unroll
+        for (int k = 0; k < R; ++k) dot2_step(s[k], cc[k], v, xs[k][0][j], xs[k][1][j]);
+    }
+    double* o = part + poff + ((long long)c * m + row) * rstride;
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (k < r) o[k] = (double)s[k] + (double)cc[k];
+}
 
 template <int R>
 __global__ void __launch_bounds__(MV_ROWS) mv_partial(const __grid_constant__ MvArgs args, double* __restrict__ part) {
@@ -155,8 +219,21 @@ void matvec_group(const std::vector<MvJob>& jobs_in, cudaStream_t st) {
         }
         DevBuf<double> part((size_t)off, st);
         const dim3 grid(ceil_div(maxm, MV_ROWS), maxc, (unsigned)a.n);
-        if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<2>, grid, MV_ROWS, 0, st, a, part.get());
-        else TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
+        bool all32 = true;
+        for (int k = 0; k < a.n; ++k) all32 = all32 && a.j[k].j.A32 != nullptr;
+        if (kstats_on()) {
+            char note[96];
+            std::snprintf(note, sizeof note, "jobs=%d m=%d chunks=%d r=%d fp32=%d", a.n, maxm, maxc, maxr, (int)all32);
+            kstat_note(note);
+        }
+        if (all32) {
+            if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<2>, grid, MV_ROWS, 0, st, a, part.get());
+            else TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
+        } else if (maxr <= 2) {
+            TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<2>, grid, MV_ROWS, 0, st, a, part.get());
+        } else {
+            TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
+        }
         LAUNCH(mv_finish, dim3(ceil_div(maxm, 128), (unsigned)a.n), 128, 0, st, a, part.get());
     }
 }

@@ -84,79 +84,173 @@ __device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x
 // LU of the block without exchanges, flagging |l| > 1 (bit 0) and a zero or
 // non-finite pivot (bit 1); then L^{-1} by forward and U^{-1} by backward
 // elimination applied to the identity.
+//
+// Each of the 512 threads keeps an 8 x 4 cyclic sub-block in registers (rows
+// tr + 16 i, columns tc + 32 k), so an elimination step only broadcasts the
+// pivot column and row through shared memory (double-buffered: one barrier per
+// step) and updates the registers; shared memory stages the coalesced loads and
+// stores of the 128 x 128 blocks.
 struct DiagArgs {
     int* flag;
     DiagJob j[MAXJOBS];
 };
 
-__global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constant__ DiagArgs args) {
-    extern __shared__ float sh[];
-    float(*a)[DP] = reinterpret_cast<float(*)[DP]>(sh);
-    float(*x)[DP] = reinterpret_cast<float(*)[DP]>(sh + MX_NB * DP);
-    const DiagJob& J = args.j[blockIdx.x];
-    int* flag = args.flag;
-    const int tid = threadIdx.x;
-    constexpr int N = MX_NB;
-    for (int e = tid; e < N * N; e += DIAG_THREADS) a[e % N][e / N] = J.A[(e % N) + (e / N) * J.lda];
-    __syncthreads();
-    int bad = 0;
-    for (int j = 0; j < N; ++j) {
-        const float piv = a[j][j];
-        if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
-        for (int i = j + 1 + tid; i < N; i += DIAG_THREADS) {
-            const float l = a[i][j] / piv;
-            a[i][j] = l;
-            if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
-        }
-        __syncthreads();
-        const int w = N - 1 - j;
-        for (int e = tid; e < w * w; e += DIAG_THREADS) {
-            const int i = j + 1 + e % w, c = j + 1 + e / w;
-            a[i][c] = fmaf(-a[i][j], a[j][c], a[i][c]);
-        }
-        __syncthreads();
+constexpr int DG_R = 16, DG_C = 32;  // thread grid: row groups x column groups
+constexpr int DG_RI = MX_NB / DG_R;  // 8 rows per thread
+constexpr int DG_CK = MX_NB / DG_C;  // 4 columns per thread
+static_assert(DG_R * DG_C == DIAG_THREADS, "diag thread grid");
+
+// register-array element selection with compile-time indices only (a runtime
+// index would move the array to local memory)
+__device__ __forceinline__ float pick_col(const float (&v)[DG_RI][DG_CK], int i, int kj) {
+    float t = v[i][0];
+#pragma unroll
+    for (int k = 1; k < DG_CK; ++k)
+        if (k == kj) t = v[i][k];
+    return t;
+}
+__device__ __forceinline__ float pick_row(const float (&v)[DG_RI][DG_CK], int ij, int k) {
+    float t = v[0][k];
+#pragma unroll
+    for (int i = 1; i < DG_RI; ++i)
+        if (i == ij) t = v[i][k];
+    return t;
+}
+// broadcast column j and row j of the distributed block v into cb / rb
+__device__ __forceinline__ void publish(const float (&cv)[DG_RI][DG_CK], const float (&rv)[DG_RI][DG_CK], int j,
+                                       int tr, int tc, float* cb, float* rb) {
+    if (tc == j % DG_C) {
+#pragma unroll
+        for (int i = 0; i < DG_RI; ++i) cb[tr + DG_R * i] = pick_col(cv, i, j / DG_C);
     }
-    if (bad) atomicOr(flag, bad);
-    for (int e = tid; e < N * N; e += DIAG_THREADS) J.A[(e % N) + (e / N) * J.lda] = a[e % N][e / N];
-    // L^{-1}
-    for (int e = tid; e < N * N; e += DIAG_THREADS) x[e / N][e % N] = (e / N == e % N) ? 1.f : 0.f;
-    __syncthreads();
-    for (int j = 0; j < N - 1; ++j) {
-        const int w = N - 1 - j;
-        for (int e = tid; e < w * (j + 1); e += DIAG_THREADS) {
-            const int i = j + 1 + e % w, c = e / w;
-            x[i][c] = fmaf(-a[i][j], x[j][c], x[i][c]);
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < N * N; e += DIAG_THREADS) {
-        const int r = e % N, c = e / N;
-        J.Li[r + c * N] = x[r][c];
-        put_split(J.LiRh, J.LiRl, (long long)r * N + c, x[r][c]);
-    }
-    __syncthreads();
-    // U^{-1}
-    for (int e = tid; e < N * N; e += DIAG_THREADS) x[e / N][e % N] = (e / N == e % N) ? 1.f : 0.f;
-    __syncthreads();
-    for (int j = N - 1; j >= 0; --j) {
-        const float d = a[j][j];
-        for (int c = j + tid; c < N; c += DIAG_THREADS) x[j][c] = x[j][c] / d;
-        __syncthreads();
-        for (int e = tid; e < j * (N - j); e += DIAG_THREADS) {
-            const int i = e % j, c = j + e / j;
-            x[i][c] = fmaf(-a[i][j], x[j][c], x[i][c]);
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < N * N; e += DIAG_THREADS) {
-        const int r = e % N, c = e / N;
-        J.Ui[r + c * N] = x[r][c];
-        put_split(J.UiRh, J.UiRl, (long long)r * N + c, x[r][c]);
-        put_split(J.UiCh, J.UiCl, (long long)c * N + r, x[r][c]);
+    if (tr == j % DG_R) {
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) rb[tc + DG_C * k] = pick_row(rv, j / DG_R, k);
     }
 }
 
-constexpr int DIAG_SMEM = 2 * MX_NB * DP * (int)sizeof(float);
+__global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constant__ DiagArgs args) {
+    extern __shared__ float sh[];
+    float(*a)[DP] = reinterpret_cast<float(*)[DP]>(sh);
+    __shared__ float colb[2][MX_NB], rowb[2][MX_NB];
+    const DiagJob& J = args.j[blockIdx.x];
+    const int tid = threadIdx.x, tr = tid % DG_R, tc = tid / DG_R;
+    constexpr int N = MX_NB;
+    for (int e = tid; e < N * N; e += DIAG_THREADS) a[e % N][e / N] = J.A[(e % N) + (e / N) * J.lda];
+    __syncthreads();
+    float v[DG_RI][DG_CK];
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) v[i][k] = a[tr + DG_R * i][tc + DG_C * k];
+    int bad = 0;
+    // ---- LU: step j broadcasts column j and row j, every thread updates its block
+    for (int j = 0; j < N; ++j) {
+        const int b = j & 1;
+        publish(v, v, j, tr, tc, colb[b], rowb[b]);
+        __syncthreads();
+        const float piv = rowb[b][j];
+        if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+        const float rp = 1.f / piv;
+        float u[DG_CK];  // row j right of the pivot (0 elsewhere: those entries stay unchanged)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) u[k] = tc + DG_C * k > j ? rowb[b][tc + DG_C * k] : 0.f;
+#pragma unroll
+        for (int i = 0; i < DG_RI; ++i) {
+            const int r = tr + DG_R * i;
+            const float l = r > j ? colb[b][r] * rp : 0.f;
+            if (r > j && tc == j % DG_C) {
+#pragma unroll
+                for (int k = 0; k < DG_CK; ++k)
+                    if (k == j / DG_C) v[i][k] = l;
+                if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+            }
+#pragma unroll
+            for (int k = 0; k < DG_CK; ++k) v[i][k] = fmaf(-l, u[k], v[i][k]);
+        }
+    }
+    if (bad) atomicOr(args.flag, bad);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = v[i][k];
+    __syncthreads();
+    for (int e = tid; e < N * N; e += DIAG_THREADS) J.A[(e % N) + (e / N) * J.lda] = a[e % N][e / N];
+    // ---- L^{-1}: X = I; step j: X(i, :) -= L(i, j) X(j, :) for i > j
+    float x[DG_RI][DG_CK];
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) x[i][k] = (tr + DG_R * i == tc + DG_C * k) ? 1.f : 0.f;
+    for (int j = 0; j < N - 1; ++j) {
+        const int b = j & 1;
+        publish(v, x, j, tr, tc, colb[b], rowb[b]);
+        __syncthreads();
+        float u[DG_CK];
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) u[k] = rowb[b][tc + DG_C * k];
+#pragma unroll
+        for (int i = 0; i < DG_RI; ++i) {
+            const int r = tr + DG_R * i;
+            const float l = r > j ? colb[b][r] : 0.f;
+#pragma unroll
+            for (int k = 0; k < DG_CK; ++k) x[i][k] = fmaf(-l, u[k], x[i][k]);
+        }
+    }
+    __syncthreads();  // every read of `a` (the factor store) is done
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = x[i][k];
+    __syncthreads();
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e % N, c = e / N;
+        J.Li[r + c * N] = a[r][c];
+    }
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e / N, c = e % N;  // row-major: consecutive threads along a row
+        put_split(J.LiRh, J.LiRl, (long long)r * N + c, a[r][c]);
+    }
+    // ---- U^{-1}: X = I; step j (descending): X(j, :) /= U(j, j), X(i, :) -= U(i, j) X(j, :) for i < j
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) x[i][k] = (tr + DG_R * i == tc + DG_C * k) ? 1.f : 0.f;
+    for (int j = N - 1; j >= 0; --j) {
+        const int b = j & 1;
+        publish(v, x, j, tr, tc, colb[b], rowb[b]);
+        __syncthreads();
+        const float rd = 1.f / colb[b][j];
+        float sk[DG_CK];
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) sk[k] = rowb[b][tc + DG_C * k] * rd;
+#pragma unroll
+        for (int i = 0; i < DG_RI; ++i) {
+            const int r = tr + DG_R * i;
+            const float u = r < j ? colb[b][r] : 0.f;
+#pragma unroll
+            for (int k = 0; k < DG_CK; ++k) x[i][k] = r == j ? sk[k] : fmaf(-u, sk[k], x[i][k]);
+        }
+    }
+    __syncthreads();  // every read of `a` (the L^{-1} stores) is done
+#pragma unroll
+    for (int i = 0; i < DG_RI; ++i)
+#pragma unroll
+        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = x[i][k];
+    __syncthreads();
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e % N, c = e / N;
+        J.Ui[r + c * N] = a[r][c];
+        put_split(J.UiCh, J.UiCl, (long long)c * N + r, a[r][c]);
+    }
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e / N, c = e % N;
+        put_split(J.UiRh, J.UiRl, (long long)r * N + c, a[r][c]);
+    }
+}
+
+constexpr int DIAG_SMEM = MX_NB * DP * (int)sizeof(float);
 
 void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
     static bool attr = false;

@@ -1,6 +1,8 @@
 // stats.cu -- transfer counters and opt-in per-kernel-class event timing.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -16,7 +18,7 @@ std::atomic<long long> g_h2d_bytes{0}, g_d2h_bytes{0};
 namespace {
 struct Pending {
     cudaEvent_t a = nullptr, b = nullptr;
-    std::string cls;
+    std::string cls, note;
     double flops = 0, bytes = 0;
 };
 struct Agg {
@@ -28,6 +30,10 @@ std::atomic<bool> g_on{false};
 std::vector<Pending> g_pending;
 std::map<std::string, Agg> g_agg;
 std::vector<cudaEvent_t> g_free;  // recorded-and-collected events, reused
+// Per-launch log (profiling aid): with kernel stats enabled and SQBEM_KSTATS_LOG
+// naming a file, every timed launch appends "class microseconds flops bytes note".
+FILE* g_log = nullptr;
+thread_local std::string t_note;
 
 cudaEvent_t take_event() {
     if (!g_free.empty()) {
@@ -51,6 +57,9 @@ void collect_locked() {
                 g.seconds += ms * 1e-3;
                 g.flops += p.flops;
                 g.bytes += p.bytes;
+                if (g_log)
+                    std::fprintf(g_log, "%s %.3f %.6g %.6g %s\n", p.cls.c_str(), ms * 1e3, p.flops, p.bytes,
+                                 p.note.c_str());
             }
         }
         if (p.a) g_free.push_back(p.a);
@@ -80,7 +89,11 @@ void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double 
     p.cls = cls;
     p.flops = flops;
     p.bytes = bytes;
+    p.note.swap(t_note);
+    t_note.clear();
 }
+
+void kstat_note(const std::string& note) { t_note = note; }
 
 }  // namespace sqbem
 
@@ -97,6 +110,12 @@ extern "C" int sqbem_kernel_stats_enable(int on) {
         std::lock_guard<std::mutex> lk(g_mu);
         collect_locked();
         if (on) g_agg.clear();
+        if (g_log) {
+            std::fclose(g_log);
+            g_log = nullptr;
+        }
+        const char* path = std::getenv("SQBEM_KSTATS_LOG");
+        if (on && path && *path) g_log = std::fopen(path, "a");
         g_on.store(on != 0);
     });
 }

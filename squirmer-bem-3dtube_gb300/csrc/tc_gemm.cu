@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <mutex>
 #include <vector>
 
@@ -72,16 +73,20 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase of the given parity; false (and *err = 1) on expiry
-// or if another role already gave up.
+// or if another role already gave up.  The error flag (a global load) and the
+// clock are polled only every 64 tries: a global load inside every poll would
+// delay the reaction to a completed phase by an L2 round trip.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
-    for (;;) {
+    for (int it = 1;; ++it) {
         if (mbar_try(bar, parity)) return true;
-        if (*(volatile int*)err) return false;
-        if (clock64() - t0 > WAIT_CYCLES) {
-            atomicExch(err, 1);
-            return false;
+        if ((it & 63) == 0) {
+            if (*(volatile int*)err) return false;
+            if (clock64() - t0 > WAIT_CYCLES) {
+                atomicExch(err, 1);
+                return false;
+            }
         }
     }
 }
@@ -290,8 +295,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             const TcProblem& P = args.probs[p];
             const int local = t - P.tile_start;
             const int tm = local / P.tiles_n, tn = local % P.tiles_n;
-            if (!mbar_wait(tfull0 + 8 * acc, aph, err)) break;
-            tc_fence_after();
             // the problem's fields once per tile, in registers (parameter-space reads
             // inside the element loop cost ~30 cycles each)
             const int m = tm * BM + row;
@@ -307,42 +310,47 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             bf16* const Ph = P.P_hi;
             bf16* const Pl = P.P_lo;
             const long long prs = P.p_rs, pcs = P.p_cs;
+            const bool rd = Cp && beta != 0.f && row_ok;
+            // C of a 32-column chunk is read before any of it is written: a load
+            // issued after the previous column's store would wait for it (the
+            // compiler cannot rule out aliasing), one round trip per column.
+            // The first chunk is fetched before the accumulator is ready.
+            float cnext[32];
+            auto load_c = [&](int c0) {
+                const int n0 = tn * BN + c0;
+                const int cnt = min(32, N - n0);
+                const float* c = Cp + (long long)m * crs + (long long)n0 * ccs;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) cnext[j] = j < cnt ? c[(long long)j * ccs] : 0.f;
+            };
+            if (rd) load_c(0);
+            if (!mbar_wait(tfull0 + 8 * acc, aph, err)) break;
+            tc_fence_after();
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
+                float cv[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) cv[j] = cnext[j];
+                if (rd && c0 + 32 < BN && tn * BN + c0 + 32 < N) load_c(c0 + 32);
                 float v[32];
                 tmem_ld32(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * BN + c0), v);
                 const int n0 = tn * BN + c0;
                 const int cnt = min(32, N - n0);
                 if (!row_ok || cnt <= 0) continue;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = rd ? fmaf(beta, cv[j], alpha * v[j]) : alpha * v[j];
                 if (Cp) {
                     float* const c = Cp + (long long)m * crs + (long long)n0 * ccs;
                     if (ccs == 1 && cnt == 32 && ((uintptr_t)c & 15) == 0) {
                         // this thread's 32 columns are contiguous (row-major C)
 #pragma unroll
-                        for (int j = 0; j < 32; j += 4) {
-                            float4 y = make_float4(alpha * v[j], alpha * v[j + 1], alpha * v[j + 2], alpha * v[j + 3]);
-                            if (beta != 0.f) {
-                                const float4 o = *reinterpret_cast<const float4*>(c + j);
-                                y.x = fmaf(beta, o.x, y.x); y.y = fmaf(beta, o.y, y.y);
-                                y.z = fmaf(beta, o.z, y.z); y.w = fmaf(beta, o.w, y.w);
-                            }
-                            *reinterpret_cast<float4*>(c + j) = y;
-                            v[j] = y.x; v[j + 1] = y.y; v[j + 2] = y.z; v[j + 3] = y.w;
-                        }
+                        for (int j = 0; j < 32; j += 4)
+                            *reinterpret_cast<float4*>(c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
                     } else {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            if (j >= cnt) break;
-                            float x = alpha * v[j];
-                            float* const cj = c + (long long)j * ccs;
-                            if (beta != 0.f) x = fmaf(beta, *cj, x);
-                            *cj = x;
-                            v[j] = x;
-                        }
+                        for (int j = 0; j < 32; ++j)
+                            if (j < cnt) c[(long long)j * ccs] = v[j];
                     }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) v[j] *= alpha;
                 }
                 if (chk)
 #pragma unroll
@@ -468,6 +476,18 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
     auto flush = [&](double flops, double bytes) {
         if (a.nprob == 0) return;
         const int grid = std::min(a.total_tiles, g_num_sms);
+        if (kstats_on()) {
+            int mm = 0, mn = 0, mk = 0;
+            for (int q = 0; q < a.nprob; ++q) {
+                mm = std::max(mm, a.probs[q].M);
+                mn = std::max(mn, a.probs[q].N);
+                mk = std::max(mk, a.probs[q].K);
+            }
+            char note[128];
+            std::snprintf(note, sizeof note, "nprob=%d tiles=%d grid=%d M=%d N=%d K=%d", a.nprob, a.total_tiles, grid,
+                          mm, mn, mk);
+            kstat_note(note);
+        }
         TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
     };
     a.nprob = 0;
