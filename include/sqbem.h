@@ -62,6 +62,12 @@ int sqbem_kernel_stats(const char* cls, long long* launches, double* seconds, do
 /* comma-separated names of the classes seen so far */
 int sqbem_kernel_stats_classes(char* buf, int cap);
 
+/* Device memory: the library allocates from its own stream-ordered pool, which
+ * keeps freed memory for reuse (no re-mapping between batches).  trim_pool waits
+ * for the device and returns the cached memory to the driver.  (No counterpart
+ * in the reference, which has no device memory.) */
+int sqbem_trim_pool(void);
+
 /* ---------------------------------------------------------------- geometry
  * Host-side mesh generators; the output is bit-identical to the reference.
  * Each returns the panel count in *P.  V (9 per panel) and tags (1 per panel)

@@ -2,7 +2,10 @@
 // (a/R, beta, level, e) instances in one call, all on one stream.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -107,8 +110,23 @@ void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStr
 // member and then factored, Schur-reduced and refined with grouped launches.
 constexpr int GROUP_MAX = 48;
 
+// Host wall time per phase of the grouped mixed path, printed to stderr when
+// SQBEM_HOST_TIMING is set (profiling aid).
+struct PhaseClock {
+    bool on = std::getenv("SQBEM_HOST_TIMING") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void lap(const char* what, size_t G, int ntp, int ns) {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "host %-14s G=%zu ntp=%d Ns=%d %.2f ms\n", what, G, ntp, ns,
+                     std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
+
 void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
                double* results) {
+    PhaseClock pc;
     std::map<std::tuple<int, int, int>, std::vector<int>> groups;
     for (int k = 0; k < n; ++k) {
         const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
@@ -140,7 +158,10 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
                     tp.push_back(&t);
                 }
             }
+            const int ntp_k = std::get<1>(kv.first), ns_k = std::get<2>(kv.first);
+            pc.lap("setup", G, ntp_k, ns_k);
             if (!tp.empty()) mixed_build_tubes(tp, cx);
+            pc.lap("tubes", G, ntp_k, ns_k);
             for (size_t g = 0; g < G; ++g) {
                 const Prepared& P = prep[ids[g]];
                 sws[g] = std::make_unique<sqbem_swimmer>();
@@ -150,6 +171,7 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
                 sp.push_back(sws[g].get());
             }
             mixed_build_swimmers(sp, cx);
+            pc.lap("swimmers", G, ntp_k, ns_k);
             // the B1 = 1 and B2 = 1 slip modes of every member
             std::vector<DevBuf<double>> slip(G), xs(G);
             std::vector<const double*> in_ptr;
@@ -169,6 +191,7 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
             int iters = 0;
             double resid = 0;
             mixed_solve(sp, false, in_ptr, 2, x_ptr, cx, &iters, &resid);
+            pc.lap("solve", G, ntp_k, ns_k);
             std::vector<std::vector<double>> hx(G);
             for (size_t g = 0; g < G; ++g) {
                 hx[g].resize((size_t)(sws[g]->mx.nt + sws[g]->mx.nc) * 2);

@@ -86,7 +86,12 @@ int guarded(F&& f) {
     }
 }
 
-// Owning device allocation (stream-ordered).
+// The library's stream-ordered device pool (keeps freed memory) and the
+// host-to-device copy through pinned staging (memory.cu).
+cudaMemPool_t device_pool();
+void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
+// Owning device allocation (stream-ordered, from device_pool()).
 template <class T>
 struct DevBuf {
     T* p = nullptr;
@@ -107,7 +112,7 @@ struct DevBuf {
         st = s;
         n = count;
         if (count == 0) return;
-        cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), s);
+        cudaError_t e = cudaMallocFromPoolAsync((void**)&p, count * sizeof(T), device_pool(), s);
         if (e != cudaSuccess) {
             p = nullptr;
             (void)cudaGetLastError();
@@ -123,10 +128,7 @@ struct DevBuf {
         p = nullptr;
         n = 0;
     }
-    void upload(const T* h, size_t count) {
-        CUDA_CHECK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
-        count_h2d(count * sizeof(T));
-    }
+    void upload(const T* h, size_t count) { upload_bytes(p, h, count * sizeof(T), st); }
     void download(T* h, size_t count) const {
         CUDA_CHECK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, st));
         count_d2h(count * sizeof(T));

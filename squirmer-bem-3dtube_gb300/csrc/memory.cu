@@ -1,0 +1,107 @@
+// memory.cu -- the library's device memory pool and pinned upload staging.
+//
+// Device buffers come from one stream-ordered pool per device that keeps freed
+// memory (release threshold = max): the default pool returns it to the driver
+// at every synchronisation, and the next large allocation then has to map
+// fresh pages while the GPU waits.  sqbem_trim_pool() gives the cached memory
+// back.
+//
+// Host-to-device copies of more than a few kilobytes from pageable memory can
+// wait for the stream to drain; they go through pinned staging blocks instead
+// (copied on the host, then a truly asynchronous DMA).  A block is reused once
+// the event recorded after its copy has completed.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <deque>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace sqbem {
+
+namespace {
+
+constexpr int MAX_DEV = 64;
+cudaMemPool_t g_pools[MAX_DEV] = {};
+std::once_flag g_pool_once[MAX_DEV];
+
+struct Pinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+};
+std::mutex g_pin_mu;
+std::deque<Pinned> g_pinned;  // deque: references stay valid as it grows
+size_t g_pinned_total = 0;
+constexpr size_t PINNED_CAP = 1ull << 30;      // at most 1 GiB of staging
+constexpr size_t INLINE_BYTES = 64 * 1024;      // small copies stay direct
+
+}  // namespace
+
+cudaMemPool_t device_pool() {
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= MAX_DEV) fail(SQBEM_ERR_ARG, "device ordinal %d out of range", dev);
+    std::call_once(g_pool_once[dev], [dev] {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        CUDA_CHECK(cudaMemPoolCreate(&g_pools[dev], &props));
+        unsigned long long keep = ~0ull;
+        CUDA_CHECK(cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+    });
+    return g_pools[dev];
+}
+
+void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    count_h2d(bytes);
+    if (bytes <= INLINE_BYTES) {
+        CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return;
+    }
+    Pinned* blk = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        for (Pinned& b : g_pinned) {
+            if (b.busy && cudaEventQuery(b.ev) == cudaSuccess) b.busy = false;
+            if (!b.busy && b.bytes >= bytes && (!blk || b.bytes < blk->bytes)) blk = &b;
+        }
+        if (!blk && g_pinned_total + bytes <= PINNED_CAP) {
+            Pinned b;
+            size_t sz = 1u << 20;
+            while (sz < bytes) sz <<= 1;
+            if (cudaMallocHost(&b.p, sz) == cudaSuccess) {
+                b.bytes = sz;
+                CUDA_CHECK(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming));
+                g_pinned_total += sz;
+                g_pinned.push_back(b);
+                blk = &g_pinned.back();
+            } else {
+                (void)cudaGetLastError();
+            }
+        }
+        if (blk) blk->busy = true;
+    }
+    if (!blk) {  // staging full: the plain copy is still correct
+        CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+        return;
+    }
+    std::memcpy(blk->p, src, bytes);
+    CUDA_CHECK(cudaMemcpyAsync(dst, blk->p, bytes, cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaEventRecord(blk->ev, st));
+}
+
+}  // namespace sqbem
+
+using namespace sqbem;
+
+extern "C" int sqbem_trim_pool(void) {
+    return guarded([&] {
+        require_device();
+        CUDA_CHECK(cudaDeviceSynchronize());
+        CUDA_CHECK(cudaMemPoolTrimTo(device_pool(), 0));
+    });
+}

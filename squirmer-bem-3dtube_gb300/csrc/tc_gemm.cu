@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -473,10 +474,13 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
         CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     }
     KArgs a;
+    auto h0 = std::chrono::steady_clock::now();
     auto flush = [&](double flops, double bytes) {
         if (a.nprob == 0) return;
         const int grid = std::min(a.total_tiles, g_num_sms);
         if (kstats_on()) {
+            const double host_us =
+                std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - h0).count();
             int mm = 0, mn = 0, mk = 0;
             for (int q = 0; q < a.nprob; ++q) {
                 mm = std::max(mm, a.probs[q].M);
@@ -484,11 +488,12 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
                 mk = std::max(mk, a.probs[q].K);
             }
             char note[128];
-            std::snprintf(note, sizeof note, "nprob=%d tiles=%d grid=%d M=%d N=%d K=%d", a.nprob, a.total_tiles, grid,
-                          mm, mn, mk);
+            std::snprintf(note, sizeof note, "nprob=%d tiles=%d grid=%d M=%d N=%d K=%d host_us=%.1f", a.nprob,
+                          a.total_tiles, grid, mm, mn, mk, host_us);
             kstat_note(note);
         }
         TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
+        h0 = std::chrono::steady_clock::now();
     };
     a.nprob = 0;
     a.total_tiles = 0;

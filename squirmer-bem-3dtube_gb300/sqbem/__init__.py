@@ -72,6 +72,7 @@ SIGNATURES = {
     "sqbem_kernel_stats_enable": (_c_i, [_c_i]),
     "sqbem_kernel_stats": (_c_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong), _D, _D, _D]),
     "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
+    "sqbem_trim_pool": (_c_i, []),
     "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
     "sqbem_adjoint_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
     "sqbem_trajectory_defaults": (_c_i, [_VP]),
@@ -221,6 +222,11 @@ def transfer_bytes():
     h, d = ctypes.c_longlong(0), ctypes.c_longlong(0)
     _check(lib().sqbem_transfer_bytes(ctypes.byref(h), ctypes.byref(d)))
     return h.value, d.value
+
+
+def trim_pool():
+    """return the library's cached device memory to the driver"""
+    _check(lib().sqbem_trim_pool())
 
 
 def kernel_stats_enable(on=True):
