@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--instances", type=int, default=0,
                     help="first N instances of the workload only (small cases for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison sample")
     return ap.parse_args()
 
 
@@ -294,6 +295,38 @@ def main():
                     "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
                     "share_of_gpu_time": secs / gpu_s if gpu_s > 0 else None,
                     "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe"}
+    # assembly throughput: far-kernel flops are credited at 7 x FLOPS_PER_EVAL (= 64,
+    # csrc/assemble.cuh) per (target, panel) pair
+    assembly = None
+    if "assemble_far" in stats:
+        _, s_far, f_far, b_far = stats["assemble_far"]
+        s_near = stats.get("assemble_near", (0, 0.0, 0.0, 0.0))[1]
+        pairs = f_far / (7 * 64)
+        assembly = {"panel_pairs_per_step": pairs / args.steps, "pairs_per_s": pairs / (s_far + s_near),
+                    "far_kernel_written_gbs": b_far / s_far / 1e9,
+                    "far_kernel_frac_of_hbm": b_far / s_far / 1e9 / peaks["hbm_gbs"],
+                    "seconds_far_near": [s_far, s_near]}
+    # plain FP64 GPU path on the same workload: per-level samples, projected to
+    # the workload's level mix; the mixed results are checked against it
+    fp64 = None
+    if rank == 0 and prec == sqbem.MIXED and not args.no_fp64 and args.workload == "sweep":
+        import numpy as np
+        per_level, errs = {}, []
+        for lev in sorted({i["sphere_level"] for i in insts}):
+            idx = [k for k, i in enumerate(insts) if i["sphere_level"] == lev][:6]
+            sample = [insts[k] for k in idx]
+            sqbem.kinematics_batch(sample[:1], sqbem.FP64)
+            r64, s64 = sqbem.kinematics_batch(sample, sqbem.FP64)
+            per_level[lev] = s64 / len(sample)
+            for j, k in enumerate(idx):
+                a, b = results[k][:12], r64[j][:12]
+                errs.append(float(np.max(np.abs(a - b)) / np.max(np.abs(b))))
+        t64 = sum(per_level[i["sphere_level"]] for i in insts)
+        fp64 = {"value": len(insts) / t64, "unit": "solves/s",
+                "sample": "6 instances per sphere level of the same workload, FP64 GPU path, projected to its "
+                          "level mix", "seconds_per_solve_by_level": per_level,
+                "mixed_over_fp64": (solves / gpu_s) / (len(insts) / t64) if ws == 1 else None,
+                "max_rel_err_mixed_vs_fp64": max(errs)}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         n, dt, levels = cpu_sample(insts, 20.0)
@@ -313,6 +346,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
+        "assembly": assembly,
+        "fp64_gpu": fp64,
         "cpu_baseline": cpu,
         "kernel_stats": {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]}
                          for c, v in stats.items()},

@@ -30,6 +30,7 @@
 // 448-point near-singular rule and the Duffy self integrals stay FP64.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <mutex>
 #include <vector>
 
@@ -370,6 +371,11 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     if (mixed) TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
     else TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
     const int warps = 152 * 16;
+    if (kstats_on()) {
+        char note[96];
+        std::snprintf(note, sizeof note, "nT=%d nS=%d same=%d mixed=%d", job.nT, job.nS, job.same_mesh, (int)mixed);
+        kstat_note(note);
+    }
     if (mixed) TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
     else TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
     if ((long long)job.nT * job.nS > near_cap) {

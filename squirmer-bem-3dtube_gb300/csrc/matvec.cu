@@ -192,13 +192,22 @@ __global__ void sumsq_kernel(const __grid_constant__ NormArgs args) {
 
 }  // namespace
 
+static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st);
+
+// FP32 and FP64 matrices go to separate launches: one FP64 job would otherwise
+// move the whole launch onto the FP64 kernel.
 void matvec_group(const std::vector<MvJob>& jobs_in, cudaStream_t st) {
-    std::vector<MvJob> jobs;
+    std::vector<MvJob> j32, j64;
     for (const MvJob& j : jobs_in)
         if (j.m > 0 && j.r > 0) {
             if (j.r > MV_RMAX) fail(SQBEM_ERR_ARG, "matvec: at most %d right-hand sides", MV_RMAX);
-            jobs.push_back(j);
+            (j.A32 ? j32 : j64).push_back(j);
         }
+    matvec_launches(j32, st);
+    matvec_launches(j64, st);
+}
+
+static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
     for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
         MvArgs a;
         a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
