@@ -193,23 +193,57 @@ __device__ void warp_rule(Acc<T>& A, const PanelRec& P, double x, double y, doub
     warp_reduce(A);
 }
 
+// FP32 evaluation of a 7/28/112-point rule from centroid-relative offsets:
+// r = (c - x0) + sum_k l_k (V_k - c).  The FP64 differences and their FP32
+// roundings are spread over lanes 0..15 (one value each) and broadcast by
+// shuffles, so a pair costs a few FP64 warp instructions instead of a dozen
+// per lane (GB300's FP64 pipe runs at about 1/64 of the FP32 rate).
+__device__ void warp_rule_f32(Acc<float>& A, const PanelRec* Pg, double x, double y, double z, int rule, int lane) {
+    A.zero();
+    float val = 0.f;
+    if (lane < 9) val = (float)(Pg->v[lane] - Pg->c[lane % 3]);
+    else if (lane < 12) val = (float)(Pg->c[lane - 9] - (lane == 9 ? x : lane == 10 ? y : z));
+    else if (lane < 15) val = (float)Pg->n[lane - 12];
+    else if (lane == 15) val = (float)Pg->area;
+    float d[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[k] = __shfl_sync(0xffffffffu, val, k);
+    const float bx = __shfl_sync(0xffffffffu, val, 9), by = __shfl_sync(0xffffffffu, val, 10),
+                bz = __shfl_sync(0xffffffffu, val, 11);
+    const float mx = __shfl_sync(0xffffffffu, val, 12), my = __shfl_sync(0xffffffffu, val, 13),
+                mz = __shfl_sync(0xffffffffu, val, 14), area = __shfl_sync(0xffffffffu, val, 15);
+    const int q0 = rule_off(rule), q1 = rule_off(rule + 1);
+    for (int q = q0 + lane; q < q1; q += 32) {
+        const QPointF Q = d_rulef[q];
+        const float rx = bx + (Q.l0 * d[0] + Q.l1 * d[3] + Q.l2 * d[6]);
+        const float ry = by + (Q.l0 * d[1] + Q.l1 * d[4] + Q.l2 * d[7]);
+        const float rz = bz + (Q.l0 * d[2] + Q.l1 * d[5] + Q.l2 * d[8]);
+        accum<float, true>(A, rx, ry, rz, Q.w * area, mx, my, mz);
+    }
+    warp_reduce(A);
+}
+
 // Duffy self integral (kernels.hpp:50-65): x0 inside the panel; three
 // sub-triangles (x0, V_e, V_e+1), x = x0 + u[(1 - v) e1 + v e2], Jacobian u J.
+// The edge vectors and J are formed once per sub-triangle; the lanes split its
+// 10 x 10 points.
 __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y, double z, int lane) {
     A.zero();
-    for (int t = lane; t < 300; t += 32) {
-        const int e = t / 100, g = t % 100;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
         const int f = e == 2 ? 0 : e + 1;
         const double e1x = P.v[3 * e] - x, e1y = P.v[3 * e + 1] - y, e1z = P.v[3 * e + 2] - z;
         const double e2x = P.v[3 * f] - x, e2y = P.v[3 * f + 1] - y, e2z = P.v[3 * f + 2] - z;
         const double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
         const double J = sqrt(cx * cx + cy * cy + cz * cz);
-        const QPoint Q = d_duffy[g];
-        const double u = Q.l0, v = Q.l1;
-        const double rx = u * ((1 - v) * e1x + v * e2x);
-        const double ry = u * ((1 - v) * e1y + v * e2y);
-        const double rz = u * ((1 - v) * e1z + v * e2z);
-        accum<double, false>(A, rx, ry, rz, Q.w * u * J, 0.0, 0.0, 0.0);
+        for (int g = lane; g < 100; g += 32) {
+            const QPoint Q = d_duffy[g];
+            const double u = Q.l0, v = Q.l1;
+            const double rx = u * ((1 - v) * e1x + v * e2x);
+            const double ry = u * ((1 - v) * e1y + v * e2y);
+            const double rz = u * ((1 - v) * e1z + v * e2z);
+            accum<double, false>(A, rx, ry, rz, Q.w * u * J, 0.0, 0.0, 0.0);
+        }
     }
     warp_reduce(A);
 }
@@ -286,11 +320,14 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
             const double cx = P.c[0] - x, cy = P.c[1] - y, cz = P.c[2] - z;
             const double d2 = cx * cx + cy * cy + cz * cz;
             const FarF& F = sf[s];
-            bool near = self || d2 < F.far2 * (1.0 - 1e-12);
-            if (!near && !(d2 > F.far2 * (1.0 + 1e-12))) near = rule_of(P, x, y, z) != 0;
-            if (near) {
+            // exact rule only for pairs that are near or inside the band (the near
+            // kernel takes the rule from the list)
+            int rule = 0;
+            if (self) rule = 4;
+            else if (!(d2 > F.far2 * (1.0 + 1e-12))) rule = rule_of(P, x, y, z);
+            if (rule != 0) {
                 const int slot = atomicAdd(job.near_count, 1);
-                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | ((self ? 4 : 1) << 28));
+                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
                 continue;
             }
             // r = (c - x0) + sum_k l_k (V_k - c): FP64 only in the centroid offset
@@ -327,8 +364,7 @@ __global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
         const int i = e.x, p = e.y & 0x0fffffff;
         const PanelRec P = job.src[p];
         const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
-        // the far kernel may only have marked the pair as near: the exact rule here
-        const int rule = (e.y >> 28) == 4 ? 4 : rule_of(P, x, y, z);
+        const int rule = e.y >> 28;  // exact rule (4 = self), decided by the far kernel
         double sl = 0, dl = 0;
         const int a = lane / 3, b = lane % 3;
         if (rule == 4) {
@@ -337,7 +373,7 @@ __global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
             if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
         } else if (MIXED && rule < 3) {
             Acc<float> A;
-            warp_rule<float>(A, P, x, y, z, rule, lane);
+            warp_rule_f32(A, job.src + p, x, y, z, rule, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
         } else {
             Acc<double> A;
@@ -566,7 +602,7 @@ __global__ void __launch_bounds__(FIELD_WARPS * 32) field_kernel(FieldJob job) {
         double sl[9], dl[9];
         if (job.mixed && rule < 3) {
             Acc<float> A;
-            warp_rule<float>(A, P, x, y, z, rule, lane);
+            warp_rule_f32(A, job.panels + p, x, y, z, rule, lane);
             for (int q = 0; q < 9; ++q) { sl[q] = sl_entry(A, q / 3, q % 3); dl[q] = dl_entry(A, q / 3, q % 3); }
         } else {
             Acc<double> A;

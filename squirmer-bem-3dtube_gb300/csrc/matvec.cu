@@ -26,7 +26,15 @@ namespace sqbem {
 namespace {
 
 constexpr int MV_ROWS = 128;
-constexpr int MV_CHUNK = 256;
+#ifndef SQBEM_MV_CHUNK
+#define SQBEM_MV_CHUNK 128
+#endif
+#ifndef SQBEM_MV_BATCH
+#define SQBEM_MV_BATCH 8
+#endif
+constexpr int MV_CHUNK = SQBEM_MV_CHUNK;
+constexpr int MV_BATCH = SQBEM_MV_BATCH;  // matrix loads issued together before their products
+static_assert(MV_CHUNK % MV_BATCH == 0, "matvec chunk must be a multiple of the load batch");
 constexpr int MV_RMAX = 8;
 
 constexpr int MAXJOBS = 48;
@@ -91,11 +99,16 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
 #pragma unroll
     for (int k = 0; k < R; ++k) s[k] = cc[k] = 0.f;
     const float* a = A + row + (long long)j0 * lda;
-#pragma unroll 8
-    for (int j = 0; j < nj; ++j, a += lda) {
-        const float v = __ldg(a);
+    // MV_BATCH independent loads in flight per thread; entries past the chunk
+    // read as 0 (and the staged vector is 0 there), adding nothing.
+    for (int j = 0; j < nj; j += MV_BATCH) {
+        float av[MV_BATCH];
 #pragma unroll
-        for (int k = 0; k < R; ++k) dot2_step(s[k], cc[k], v, xs[k][0][j], xs[k][1][j]);
+        for (int u = 0; u < MV_BATCH; ++u) av[u] = j + u < nj ? __ldg(a + (long long)(j + u) * lda) : 0.f;
+#pragma unroll
+        for (int u = 0; u < MV_BATCH; ++u)
+#pragma unroll
+            for (int k = 0; k < R; ++k) dot2_step(s[k], cc[k], av[u], xs[k][0][j + u], xs[k][1][j + u]);
     }
     double* o = part + poff + ((long long)c * m + row) * rstride;
 #pragma unroll

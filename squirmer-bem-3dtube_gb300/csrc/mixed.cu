@@ -298,10 +298,16 @@ void run(std::vector<TcProblem>& P, std::vector<TcOperands>& O, const MixedCtx& 
 
 // TRSM with the unit-lower (lower = true) or upper factor of every member on
 // rows [k0, k0 + w), columns [j0, j0 + nc) of its target.
+// tri: the right-hand side is lower triangular from column j0 on (the identity
+// of an inversion), so in the lower solve column c of X stays zero above row c
+// and only columns c < k0 + w (relative to j0: c - j0 < k0 + w) take part.
 void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool lower, int k0, int w, int j0,
-          const std::vector<int>& ncols, const MixedCtx& cx) {
+          const std::vector<int>& ncols_in, const MixedCtx& cx, bool tri = false) {
     std::vector<TcProblem> P;
     std::vector<TcOperands> O;
+    std::vector<int> ncols = ncols_in;
+    if (tri && lower)
+        for (int& c : ncols) c = std::min(c, k0 + w);
     if (w == MX_NB) {
         // leaf: B -> split (column-major), X = inv_b * B, keep the split copies equal to X
         std::vector<ConvJob> cj;
@@ -342,23 +348,24 @@ void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool low
     // lower: first half solves, then updates the second; upper: the reverse
     const int ka = lower ? k0 : k0 + w1, wa = lower ? w1 : w2;  // solved first
     const int kb = lower ? k0 + w1 : k0, wb = lower ? w2 : w1;  // updated, solved second
-    trsm(g, T, lower, ka, wa, j0, ncols, cx);
+    trsm(g, T, lower, ka, wa, j0, ncols, cx, tri);
     for (size_t m = 0; m < g.size(); ++m) {
-        if (ncols[m] <= 0) continue;
+        const int nc = tri && lower ? std::min(ncols[m], ka + wa) : ncols[m];
+        if (nc <= 0) continue;
         MixedLU& L = *g[m];
         const Target& t = T[m];
         TcProblem p;
-        p.M = wb; p.N = ncols[m]; p.K = wa;
+        p.M = wb; p.N = nc; p.K = wa;
         p.alpha = -1.f; p.beta = 1.f;
         p.C = t.X + kb + (long long)j0 * t.ldx; p.c_rs = 1; p.c_cs = t.ldx;
         TcOperands o;
         o.A = rview(L.Rh.get(), L.Rl.get(), L.n, kb, ka, wb, wa);  // factor block (rows kb, columns ka)
-        o.B = cview(t.Ch, t.Cl, t.ldc, ka, j0, wa, ncols[m]);       // solved rows of X
+        o.B = cview(t.Ch, t.Cl, t.ldc, ka, j0, wa, nc);             // solved rows of X
         P.push_back(p);
         O.push_back(o);
     }
     run(P, O, cx);
-    trsm(g, T, lower, kb, wb, j0, ncols, cx);
+    trsm(g, T, lower, kb, wb, j0, ncols, cx, tri);
 }
 
 void leaf(const std::vector<MixedLU*>& g, int c0, const MixedCtx& cx) {
@@ -465,7 +472,8 @@ void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx) {
     lu_rec(g, 0, n, cx);
 }
 
-void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx) {
+void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx,
+                    bool identity_rhs) {
     if (g.empty()) return;
     std::vector<Target> T;
     std::vector<int> nc;
@@ -478,7 +486,7 @@ void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs,
     }
     if (maxc == 0) return;
     const int n = g[0]->n;
-    trsm(g, T, true, 0, n, 0, nc, cx);
+    trsm(g, T, true, 0, n, 0, nc, cx, identity_rhs);
     trsm(g, T, false, 0, n, 0, nc, cx);
 }
 

@@ -54,8 +54,10 @@ struct MixedCtx {
 
 // Factor every matrix of the group (A already filled, padding = identity).
 void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx);
-// X_k <- A_k^{-1} X_k for every member k.
-void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx);
+// X_k <- A_k^{-1} X_k for every member k.  identity_rhs: X_k holds the identity
+// (an inversion), whose zeros above the diagonal the lower solve skips.
+void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx,
+                    bool identity_rhs = false);
 
 // Grouped FP32 -> split-BF16 conversion.
 struct ConvJob {

@@ -147,15 +147,19 @@ static void invert_group(const std::vector<MixedLU*>& L, const std::vector<float
         const int n = L[k]->n;
         CUDA_CHECK(cudaMemsetAsync(inv[k], 0, sizeof(float) * (size_t)n * n, cx.st));
         pad_identity(inv[k], n, 0, n, cx.st);
+        // split copies start as the exact split of the identity's zeros: the lower
+        // solve skips the zero blocks above the diagonal, which later updates read
         ch[k].alloc((size_t)n * n, cx.st);
         cl[k].alloc((size_t)n * n, cx.st);
+        ch[k].zero();
+        cl[k].zero();
         Rhs& r = rhs[k];
         r.X = inv[k]; r.ldx = n; r.nrhs = n; r.Sh = ch[k].get(); r.Sl = cl[k].get(); r.lds = n;
         r.Rh = rh.empty() ? nullptr : rh[k];
         r.Rl = rl.empty() ? nullptr : rl[k];
         r.ldr = n;
     }
-    mixed_lu_solve(L, rhs, cx);
+    mixed_lu_solve(L, rhs, cx, true);
 }
 
 // ---------------------------------------------------------------- tubes
