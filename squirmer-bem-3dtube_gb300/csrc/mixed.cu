@@ -82,175 +82,139 @@ __device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x
 }
 
 // LU of the block without exchanges, flagging |l| > 1 (bit 0) and a zero or
-// non-finite pivot (bit 1); then L^{-1} by forward and U^{-1} by backward
-// elimination applied to the identity.
+// non-finite pivot (bit 1); then L^{-1} and U^{-1}.  The whole block lives in
+// shared memory (with both inverses: 3 x 128 x 129 floats).
 //
-// Each of the 512 threads keeps an 8 x 4 cyclic sub-block in registers (rows
-// tr + 16 i, columns tc + 32 k), so an elimination step only broadcasts the
-// pivot column and row through shared memory (double-buffered: one barrier per
-// step) and updates the registers; shared memory stages the coalesced loads and
-// stores of the 128 x 128 blocks.
+// LU, blocked right-looking with 16-column panels:
+//   panel   4 threads per row, each 4 of the panel's columns; one barrier per
+//           column (the multiplier is read by the row's 4 threads, which share a
+//           warp, before the one owning the pivot column overwrites it);
+//   U12     one thread per column solves with the unit-lower 16 x 16 block;
+//   A22     rank-16 update, 4 rows x 1 column per thread (columns across the
+//           warp: conflict-free; the row values are broadcasts).
+// Inverses: threads 0-255 form L^{-1} and 256-511 U^{-1}, two threads per
+// column splitting each inner sum (combined with a shuffle); only the nonzero
+// triangle of every column is visited.
 struct DiagArgs {
     int* flag;
     DiagJob j[MAXJOBS];
 };
 
-constexpr int DG_R = 16, DG_C = 32;  // thread grid: row groups x column groups
-constexpr int DG_RI = MX_NB / DG_R;  // 8 rows per thread
-constexpr int DG_CK = MX_NB / DG_C;  // 4 columns per thread
-static_assert(DG_R * DG_C == DIAG_THREADS, "diag thread grid");
-
-// register-array element selection with compile-time indices only (a runtime
-// index would move the array to local memory)
-__device__ __forceinline__ float pick_col(const float (&v)[DG_RI][DG_CK], int i, int kj) {
-    float t = v[i][0];
-#pragma unroll
-    for (int k = 1; k < DG_CK; ++k)
-        if (k == kj) t = v[i][k];
-    return t;
-}
-__device__ __forceinline__ float pick_row(const float (&v)[DG_RI][DG_CK], int ij, int k) {
-    float t = v[0][k];
-#pragma unroll
-    for (int i = 1; i < DG_RI; ++i)
-        if (i == ij) t = v[i][k];
-    return t;
-}
-// broadcast column j and row j of the distributed block v into cb / rb
-__device__ __forceinline__ void publish(const float (&cv)[DG_RI][DG_CK], const float (&rv)[DG_RI][DG_CK], int j,
-                                       int tr, int tc, float* cb, float* rb) {
-    if (tc == j % DG_C) {
-#pragma unroll
-        for (int i = 0; i < DG_RI; ++i) cb[tr + DG_R * i] = pick_col(cv, i, j / DG_C);
-    }
-    if (tr == j % DG_R) {
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) rb[tc + DG_C * k] = pick_row(rv, j / DG_R, k);
-    }
-}
+constexpr int DG_PW = 16;  // LU panel width
 
 __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constant__ DiagArgs args) {
     extern __shared__ float sh[];
-    float(*a)[DP] = reinterpret_cast<float(*)[DP]>(sh);
-    __shared__ float colb[2][MX_NB], rowb[2][MX_NB];
-    const DiagJob& J = args.j[blockIdx.x];
-    const int tid = threadIdx.x, tr = tid % DG_R, tc = tid / DG_R;
     constexpr int N = MX_NB;
-    for (int e = tid; e < N * N; e += DIAG_THREADS) a[e % N][e / N] = J.A[(e % N) + (e / N) * J.lda];
+    float(*a)[DP] = reinterpret_cast<float(*)[DP]>(sh);
+    float(*xl)[DP] = reinterpret_cast<float(*)[DP]>(sh + N * DP);
+    float(*xu)[DP] = reinterpret_cast<float(*)[DP]>(sh + 2 * N * DP);
+    float* rd = sh + 3 * N * DP;  // 1 / U(r, r)
+    const DiagJob& J = args.j[blockIdx.x];
+    const int tid = threadIdx.x;
+    {
+        const float* A = J.A;
+        const long long lda = J.lda;
+        for (int e = tid; e < N * N; e += DIAG_THREADS) a[e % N][e / N] = A[(e % N) + (e / N) * lda];
+    }
     __syncthreads();
-    float v[DG_RI][DG_CK];
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) v[i][k] = a[tr + DG_R * i][tc + DG_C * k];
     int bad = 0;
-    // ---- LU: step j broadcasts column j and row j, every thread updates its block
-    for (int j = 0; j < N; ++j) {
-        const int b = j & 1;
-        publish(v, v, j, tr, tc, colb[b], rowb[b]);
+    const int pi = tid >> 2, pg = tid & 3;  // panel step: row, quarter of the panel
+    for (int c0 = 0; c0 < N; c0 += DG_PW) {
+        for (int j = c0; j < c0 + DG_PW; ++j) {
+            const float piv = a[j][j];
+            if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+            const bool act = pi > j;
+            const float l = act ? a[pi][j] / piv : 0.f;
+            __syncwarp();
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int c = c0 + 4 * pg + q;
+                    if (c > j) {
+                        a[pi][c] = fmaf(-l, a[j][c], a[pi][c]);
+                    } else if (c == j) {
+                        a[pi][c] = l;
+                        if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        {  // U12 = L11^{-1} A12
+            const int c = c0 + DG_PW + tid;
+            if (c < N)
+                for (int r = 1; r < DG_PW; ++r) {
+                    float v = a[c0 + r][c];
+                    for (int k = 0; k < r; ++k) v = fmaf(-a[c0 + r][c0 + k], a[c0 + k][c], v);
+                    a[c0 + r][c] = v;
+                }
+        }
         __syncthreads();
-        const float piv = rowb[b][j];
-        if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
-        const float rp = 1.f / piv;
-        float u[DG_CK];  // row j right of the pivot (0 elsewhere: those entries stay unchanged)
+        const int m = N - c0 - DG_PW;  // A22 -= L21 U12
+        for (int e = tid; e < (m / 4) * m; e += DIAG_THREADS) {
+            const int c = c0 + DG_PW + e % m, i0 = c0 + DG_PW + 4 * (e / m);
+            float acc[4];
 #pragma unroll
-        for (int k = 0; k < DG_CK; ++k) u[k] = tc + DG_C * k > j ? rowb[b][tc + DG_C * k] : 0.f;
+            for (int q = 0; q < 4; ++q) acc[q] = a[i0 + q][c];
 #pragma unroll
-        for (int i = 0; i < DG_RI; ++i) {
-            const int r = tr + DG_R * i;
-            const float l = r > j ? colb[b][r] * rp : 0.f;
-            if (r > j && tc == j % DG_C) {
+            for (int k = 0; k < DG_PW; ++k) {
+                const float u = a[c0 + k][c];
 #pragma unroll
-                for (int k = 0; k < DG_CK; ++k)
-                    if (k == j / DG_C) v[i][k] = l;
-                if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+                for (int q = 0; q < 4; ++q) acc[q] = fmaf(-a[i0 + q][c0 + k], u, acc[q]);
             }
 #pragma unroll
-            for (int k = 0; k < DG_CK; ++k) v[i][k] = fmaf(-l, u[k], v[i][k]);
+            for (int q = 0; q < 4; ++q) a[i0 + q][c] = acc[q];
         }
+        __syncthreads();
     }
     if (bad) atomicOr(args.flag, bad);
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = v[i][k];
-    __syncthreads();
-    for (int e = tid; e < N * N; e += DIAG_THREADS) J.A[(e % N) + (e / N) * J.lda] = a[e % N][e / N];
-    // ---- L^{-1}: X = I; step j: X(i, :) -= L(i, j) X(j, :) for i > j
-    float x[DG_RI][DG_CK];
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) x[i][k] = (tr + DG_R * i == tc + DG_C * k) ? 1.f : 0.f;
-    for (int j = 0; j < N - 1; ++j) {
-        const int b = j & 1;
-        publish(v, x, j, tr, tc, colb[b], rowb[b]);
-        __syncthreads();
-        float u[DG_CK];
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) u[k] = rowb[b][tc + DG_C * k];
-#pragma unroll
-        for (int i = 0; i < DG_RI; ++i) {
-            const int r = tr + DG_R * i;
-            const float l = r > j ? colb[b][r] : 0.f;
-#pragma unroll
-            for (int k = 0; k < DG_CK; ++k) x[i][k] = fmaf(-l, u[k], x[i][k]);
-        }
+    {
+        float* A = J.A;
+        const long long lda = J.lda;
+        for (int e = tid; e < N * N; e += DIAG_THREADS) A[(e % N) + (e / N) * lda] = a[e % N][e / N];
     }
-    __syncthreads();  // every read of `a` (the factor store) is done
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = x[i][k];
+    for (int r = tid; r < N; r += DIAG_THREADS) rd[r] = 1.f / a[r][r];
     __syncthreads();
     for (int e = tid; e < N * N; e += DIAG_THREADS) {
         const int r = e % N, c = e / N;
-        J.Li[r + c * N] = a[r][c];
+        xl[r][c] = r == c ? 1.f : 0.f;
+        xu[r][c] = r == c ? rd[r] : 0.f;
+    }
+    __syncthreads();
+    if (tid < 2 * N) {  // L^{-1}: X(r, c) = -sum_{c <= k < r} L(r, k) X(k, c)
+        const int c = tid >> 1, h = tid & 1;
+        for (int r = 1; r < N; ++r) {
+            float v = 0.f;
+            for (int k = c + h; k < r; k += 2) v = fmaf(a[r][k], xl[k][c], v);
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            if (h == 0 && r > c) xl[r][c] = -v;
+            __syncwarp();
+        }
+    } else {  // U^{-1}: X(r, c) = -sum_{r < k <= c} U(r, k) X(k, c) / U(r, r)
+        const int c = (tid - 2 * N) >> 1, h = tid & 1;
+        for (int r = N - 2; r >= 0; --r) {
+            float v = 0.f;
+            for (int k = r + 1 + h; k <= c; k += 2) v = fmaf(a[r][k], xu[k][c], v);
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            if (h == 0 && r < c) xu[r][c] = -v * rd[r];
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < N * N; e += DIAG_THREADS) {
+        const int r = e % N, c = e / N;
+        J.Li[r + c * N] = xl[r][c];
+        J.Ui[r + c * N] = xu[r][c];
+        put_split(J.UiCh, J.UiCl, (long long)c * N + r, xu[r][c]);
     }
     for (int e = tid; e < N * N; e += DIAG_THREADS) {
         const int r = e / N, c = e % N;  // row-major: consecutive threads along a row
-        put_split(J.LiRh, J.LiRl, (long long)r * N + c, a[r][c]);
-    }
-    // ---- U^{-1}: X = I; step j (descending): X(j, :) /= U(j, j), X(i, :) -= U(i, j) X(j, :) for i < j
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) x[i][k] = (tr + DG_R * i == tc + DG_C * k) ? 1.f : 0.f;
-    for (int j = N - 1; j >= 0; --j) {
-        const int b = j & 1;
-        publish(v, x, j, tr, tc, colb[b], rowb[b]);
-        __syncthreads();
-        const float rd = 1.f / colb[b][j];
-        float sk[DG_CK];
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) sk[k] = rowb[b][tc + DG_C * k] * rd;
-#pragma unroll
-        for (int i = 0; i < DG_RI; ++i) {
-            const int r = tr + DG_R * i;
-            const float u = r < j ? colb[b][r] : 0.f;
-#pragma unroll
-            for (int k = 0; k < DG_CK; ++k) x[i][k] = r == j ? sk[k] : fmaf(-u, sk[k], x[i][k]);
-        }
-    }
-    __syncthreads();  // every read of `a` (the L^{-1} stores) is done
-#pragma unroll
-    for (int i = 0; i < DG_RI; ++i)
-#pragma unroll
-        for (int k = 0; k < DG_CK; ++k) a[tr + DG_R * i][tc + DG_C * k] = x[i][k];
-    __syncthreads();
-    for (int e = tid; e < N * N; e += DIAG_THREADS) {
-        const int r = e % N, c = e / N;
-        J.Ui[r + c * N] = a[r][c];
-        put_split(J.UiCh, J.UiCl, (long long)c * N + r, a[r][c]);
-    }
-    for (int e = tid; e < N * N; e += DIAG_THREADS) {
-        const int r = e / N, c = e % N;
-        put_split(J.UiRh, J.UiRl, (long long)r * N + c, a[r][c]);
+        put_split(J.LiRh, J.LiRl, (long long)r * N + c, xl[r][c]);
+        put_split(J.UiRh, J.UiRl, (long long)r * N + c, xu[r][c]);
     }
 }
 
-constexpr int DIAG_SMEM = MX_NB * DP * (int)sizeof(float);
+constexpr int DIAG_SMEM = (3 * MX_NB * DP + MX_NB) * (int)sizeof(float);
 
 void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
     static bool attr = false;
