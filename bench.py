@@ -99,7 +99,7 @@ class Clocks:
         os.close(fd)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,memory.used")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
@@ -131,6 +131,8 @@ class Clocks:
                     reasons.add(nm)
         out["reasons"] = sorted(reasons)
         out["samples"] = len(rows)
+        mem = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
+        out["device_mem_peak_mib"] = max(mem) if mem else None
         return out
 
 
@@ -281,20 +283,40 @@ def main():
     # dominant kernel class of the timed region
     stats = {c: sqbem.kernel_stats(c) for c in sqbem.kernel_stats_classes()}
     sqbem.kernel_stats_enable(False)
-    top = max(stats, key=lambda c: stats[c][1]) if stats else None
-    roofline = None
-    if top:
-        nl, secs, fl, by = stats[top]
+
+    def roofline_of(st, note):
+        top = max(st, key=lambda c: st[c][1]) if st else None
+        if not top:
+            return None
+        nl, secs, fl, by = st[top]
         if top in ("tc_gemm",):
             achieved, peak, unit, bound = fl / secs / 1e12, peaks["bf16_tflops"], "TFLOP/s", "tensor"
         elif top == "dgemm":
             achieved, peak, unit, bound = fl / secs / 1e12, FP64_PEAK_TFLOPS, "TFLOP/s (fp64)", "tensor"
         else:
             achieved, peak, unit, bound = by / secs / 1e9, peaks["hbm_gbs"], "GB/s", "hbm"
-        roofline = {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                    "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
-                    "share_of_gpu_time": secs / gpu_s if gpu_s > 0 else None,
-                    "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe"}
+        return {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
+                "launch_seconds": secs, "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe",
+                "note": note}
+
+    roofline = roofline_of(stats, "per-launch CUDA events over the timed region; with concurrent streams a "
+                                  "launch's duration includes the kernels of other streams sharing the GPU")
+    # the same classes from one extra, untimed step on a single stream: the
+    # kernels' own rates, without co-scheduling
+    roofline_1s = None
+    if rank == 0 and args.impl == "gb300":
+        prev = os.environ.get("SQBEM_STREAMS")
+        os.environ["SQBEM_STREAMS"] = "1"
+        sqbem.kernel_stats_enable(True)
+        sqbem.kinematics_batch(insts, prec)
+        st1 = {c: sqbem.kernel_stats(c) for c in sqbem.kernel_stats_classes()}
+        sqbem.kernel_stats_enable(False)
+        if prev is None:
+            del os.environ["SQBEM_STREAMS"]
+        else:
+            os.environ["SQBEM_STREAMS"] = prev
+        roofline_1s = roofline_of(st1, "one untimed step on a single stream, per-launch CUDA events")
     # assembly throughput: far-kernel flops are credited at 7 x FLOPS_PER_EVAL (= 64,
     # csrc/assemble.cuh) per (target, panel) pair
     assembly = None
@@ -346,6 +368,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
+        "roofline_single_stream": roofline_1s,
         "assembly": assembly,
         "fp64_gpu": fp64,
         "cpu_baseline": cpu,

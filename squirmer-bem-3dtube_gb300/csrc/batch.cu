@@ -7,7 +7,13 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <exception>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <memory>
 #include <tuple>
 #include <vector>
@@ -108,7 +114,13 @@ void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStr
 // Mixed precision: instances with equal padded tube size and equal sphere size
 // form a group; each group (in chunks of GROUP_MAX) is assembled member by
 // member and then factored, Schur-reduced and refined with grouped launches.
-constexpr int GROUP_MAX = 48;
+// Members per chunk: SQBEM_GROUP_MAX, default 48 (at most 48 problems per
+// grouped GEMM launch).
+int group_max() {
+    const char* e = std::getenv("SQBEM_GROUP_MAX");
+    const int v = e ? std::atoi(e) : 48;
+    return std::max(1, std::min(v, 48));
+}
 
 // Host wall time per phase of the grouped mixed path, printed to stderr when
 // SQBEM_HOST_TIMING is set (profiling aid).
@@ -124,132 +136,250 @@ struct PhaseClock {
     }
 };
 
+// One chunk of a group (members with equal padded tube size and sphere size),
+// everything on stream bs.
+void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_instance* inst,
+               const std::vector<Prepared>& prep, cudaStream_t bs, double* results, PhaseClock& pc) {
+    const size_t G = ids.size();
+    DevBuf<int> flags(2, bs);
+    flags.zero();
+    MixedCtx cx{bs, flags.get(), flags.get() + 1};
+    std::vector<std::unique_ptr<sqbem_tube>> tubes(G);
+    std::vector<std::unique_ptr<sqbem_swimmer>> sws(G);
+    std::vector<sqbem_tube*> tp;
+    std::vector<sqbem_swimmer*> sp;
+    for (size_t g = 0; g < G; ++g) {
+        const Prepared& P = prep[ids[g]];
+        const sqbem_instance& in = inst[ids[g]];
+        if (P.bounded) {
+            tubes[g] = std::make_unique<sqbem_tube>();
+            sqbem_tube& t = *tubes[g];
+            t.st.borrow(bs);
+            t.R = P.R; t.L = P.L; t.a = 1.0; t.n_theta = in.n_theta; t.n_r = in.n_r; t.mu = 1.0;
+            t.precision = SQBEM_MIXED;
+            t.mesh = P.tube;
+            t.set_panels();
+            tp.push_back(&t);
+        }
+    }
+    pc.lap("setup", G, ntp_k, ns_k);
+    if (!tp.empty()) mixed_build_tubes(tp, cx);
+    pc.lap("tubes", G, ntp_k, ns_k);
+    for (size_t g = 0; g < G; ++g) {
+        const Prepared& P = prep[ids[g]];
+        sws[g] = std::make_unique<sqbem_swimmer>();
+        sws[g]->st.borrow(bs);
+        const double c[3] = {P.b, 0, 0};
+        sws[g]->set_geometry(tubes[g].get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_MIXED);
+        sp.push_back(sws[g].get());
+    }
+    mixed_build_swimmers(sp, cx);
+    pc.lap("swimmers", G, ntp_k, ns_k);
+    // the B1 = 1 and B2 = 1 slip modes of every member
+    std::vector<DevBuf<double>> slip(G), xs(G);
+    std::vector<const double*> in_ptr;
+    std::vector<double*> x_ptr;
+    for (size_t g = 0; g < G; ++g) {
+        sqbem_swimmer& s = *sws[g];
+        const double c[3] = {prep[ids[g]].b, 0, 0};
+        auto u1 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 1, 0);
+        const auto u2 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 0, 1);
+        u1.insert(u1.end(), u2.begin(), u2.end());
+        slip[g].alloc(u1.size(), bs);
+        slip[g].upload(u1.data(), u1.size());
+        xs[g].alloc((size_t)(s.mx.nt + s.mx.nc) * 2, bs);
+        in_ptr.push_back(slip[g].get());
+        x_ptr.push_back(xs[g].get());
+    }
+    int iters = 0;
+    double resid = 0;
+    mixed_solve(sp, false, in_ptr, 2, x_ptr, cx, &iters, &resid);
+    pc.lap("solve", G, ntp_k, ns_k);
+    std::vector<std::vector<double>> hx(G);
+    for (size_t g = 0; g < G; ++g) {
+        hx[g].resize((size_t)(sws[g]->mx.nt + sws[g]->mx.nc) * 2);
+        xs[g].download(hx[g].data(), hx[g].size());
+    }
+    // towed drag of the members on the axis (main.cpp:90-91)
+    std::vector<sqbem_swimmer*> towed;
+    std::vector<size_t> towed_g;
+    for (size_t g = 0; g < G; ++g)
+        if (inst[ids[g]].towed && std::fabs(prep[ids[g]].b) < 1e-12) {
+            towed.push_back(sws[g].get());
+            towed_g.push_back(g);
+        }
+    std::vector<std::vector<double>> hf(towed.size());
+    if (!towed.empty()) {
+        const double w6[6] = {0, 0, 1, 0, 0, 0};
+        DevBuf<double> dw(6, bs);
+        dw.upload(w6, 6);
+        std::vector<DevBuf<double>> xt(towed.size());
+        std::vector<const double*> wi;
+        std::vector<double*> xo;
+        for (size_t t = 0; t < towed.size(); ++t) {
+            xt[t].alloc((size_t)(towed[t]->mx.nt + towed[t]->mx.nc), bs);
+            wi.push_back(dw.get());
+            xo.push_back(xt[t].get());
+        }
+        int it2 = 0;
+        double r2 = 0;
+        mixed_solve(towed, true, wi, 1, xo, cx, &it2, &r2);
+        for (size_t t = 0; t < towed.size(); ++t) {
+            hf[t].resize(xt[t].n);
+            xt[t].download(hf[t].data(), hf[t].size());
+        }
+    }
+    CUDA_CHECK(cudaStreamSynchronize(bs));
+    for (size_t g = 0; g < G; ++g) {
+        sqbem_swimmer& s = *sws[g];
+        const int nt = s.mx.nt, ns = s.mx.ns, ldx = nt + s.mx.nc;
+        double* res = results + (size_t)ids[g] * SQBEM_RESULT_STRIDE;
+        for (int c = 0; c < 3; ++c) {
+            res[c] = hx[g][nt + ns + c];
+            res[3 + c] = hx[g][nt + ns + 3 + c];
+            res[6 + c] = hx[g][ldx + nt + ns + c];
+            res[9 + c] = hx[g][ldx + nt + ns + 3 + c];
+        }
+        res[12] = NAN;
+        res[13] = s.Nt;
+        res[14] = s.Ns;
+        res[15] = iters;
+    }
+    for (size_t t = 0; t < towed.size(); ++t) {
+        sqbem_swimmer& s = *towed[t];
+        double Fz = 0;
+        for (int p = 0; p < s.Ns; ++p) Fz = Fz - s.host_panels[p].area * hf[t][s.mx.nt + 3 * p + 2];
+        results[(size_t)ids[towed_g[t]] * SQBEM_RESULT_STRIDE + 12] = -Fz / (6 * bem::PI);
+    }
+}
+
+// Chunks run concurrently: SQBEM_STREAMS host threads (default 2), each with
+// its own stream, take chunks from a shared queue (the larger spheres first),
+// so that one chunk's latency-bound phases (diagonal LU leaves, small
+// updates, host synchronisations) overlap another's large GEMMs.  The batch
+// stream's events bracket all of them.
+int stream_count() {
+    const char* e = std::getenv("SQBEM_STREAMS");
+    const int v = e ? std::atoi(e) : 6;
+    return std::max(1, std::min(v, 8));
+}
+
+// Device bytes a chunk holds at its peak, estimated from its sizes (FP32 tube
+// block, inverse and split copies; swimmer blocks B, A_uBt, D, E, A_uBs, Y,
+// G_s^{-1}; the LU working set), with a margin.
+double chunk_bytes(size_t G, int ntp, int ns) {
+    const double t = ntp, s = pad128(3 * ns);
+    return 1.25 * G * 4.0 * (6.0 * t * t + 6.0 * t * s + 5.0 * s * s);
+}
+
+// Concurrent chunks share a memory budget: free device memory plus what the
+// library's pool holds unused, times 0.8.  A chunk waits while its estimate
+// does not fit next to the running ones (one chunk always runs).
+class MemBudget {
+public:
+    explicit MemBudget(double budget) : budget_(budget) {}
+    void acquire(double b) {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return used_ == 0 || used_ + b <= budget_; });
+        used_ += b;
+    }
+    void release(double b) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            used_ -= b;
+        }
+        cv_.notify_all();
+    }
+
+private:
+    std::mutex mu_;
+    std::condition_variable cv_;
+    double budget_, used_ = 0;
+};
+
+double device_budget() {
+    size_t fr = 0, tot = 0;
+    CUDA_CHECK(cudaMemGetInfo(&fr, &tot));
+    cuuint64_t reserved = 0, in_use = 0;
+    cudaMemPool_t pool = device_pool();
+    CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+    CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &in_use));
+    return 0.8 * ((double)fr + (double)(reserved > in_use ? reserved - in_use : 0));
+}
+
 void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
                double* results) {
-    PhaseClock pc;
     std::map<std::tuple<int, int, int>, std::vector<int>> groups;
     for (int k = 0; k < n; ++k) {
         const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
         groups[{prep[k].bounded ? 1 : 0, ntp, prep[k].sphere.P()}].push_back(k);
     }
-    DevBuf<int> flags(2, bs);
+    struct Chunk {
+        std::vector<int> ids;
+        int ntp, ns;
+    };
+    std::vector<Chunk> chunks;
     for (auto& kv : groups) {
         const std::vector<int>& all = kv.second;
-        for (size_t c0 = 0; c0 < all.size(); c0 += GROUP_MAX) {
-            const std::vector<int> ids(all.begin() + c0, all.begin() + std::min(all.size(), c0 + GROUP_MAX));
-            const size_t G = ids.size();
-            flags.zero();
-            MixedCtx cx{bs, flags.get(), flags.get() + 1};
-            std::vector<std::unique_ptr<sqbem_tube>> tubes(G);
-            std::vector<std::unique_ptr<sqbem_swimmer>> sws(G);
-            std::vector<sqbem_tube*> tp;
-            std::vector<sqbem_swimmer*> sp;
-            for (size_t g = 0; g < G; ++g) {
-                const Prepared& P = prep[ids[g]];
-                const sqbem_instance& in = inst[ids[g]];
-                if (P.bounded) {
-                    tubes[g] = std::make_unique<sqbem_tube>();
-                    sqbem_tube& t = *tubes[g];
-                    t.st.borrow(bs);
-                    t.R = P.R; t.L = P.L; t.a = 1.0; t.n_theta = in.n_theta; t.n_r = in.n_r; t.mu = 1.0;
-                    t.precision = SQBEM_MIXED;
-                    t.mesh = P.tube;
-                    t.set_panels();
-                    tp.push_back(&t);
-                }
-            }
-            const int ntp_k = std::get<1>(kv.first), ns_k = std::get<2>(kv.first);
-            pc.lap("setup", G, ntp_k, ns_k);
-            if (!tp.empty()) mixed_build_tubes(tp, cx);
-            pc.lap("tubes", G, ntp_k, ns_k);
-            for (size_t g = 0; g < G; ++g) {
-                const Prepared& P = prep[ids[g]];
-                sws[g] = std::make_unique<sqbem_swimmer>();
-                sws[g]->st.borrow(bs);
-                const double c[3] = {P.b, 0, 0};
-                sws[g]->set_geometry(tubes[g].get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_MIXED);
-                sp.push_back(sws[g].get());
-            }
-            mixed_build_swimmers(sp, cx);
-            pc.lap("swimmers", G, ntp_k, ns_k);
-            // the B1 = 1 and B2 = 1 slip modes of every member
-            std::vector<DevBuf<double>> slip(G), xs(G);
-            std::vector<const double*> in_ptr;
-            std::vector<double*> x_ptr;
-            for (size_t g = 0; g < G; ++g) {
-                sqbem_swimmer& s = *sws[g];
-                const double c[3] = {prep[ids[g]].b, 0, 0};
-                auto u1 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 1, 0);
-                const auto u2 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 0, 1);
-                u1.insert(u1.end(), u2.begin(), u2.end());
-                slip[g].alloc(u1.size(), bs);
-                slip[g].upload(u1.data(), u1.size());
-                xs[g].alloc((size_t)(s.mx.nt + s.mx.nc) * 2, bs);
-                in_ptr.push_back(slip[g].get());
-                x_ptr.push_back(xs[g].get());
-            }
-            int iters = 0;
-            double resid = 0;
-            mixed_solve(sp, false, in_ptr, 2, x_ptr, cx, &iters, &resid);
-            pc.lap("solve", G, ntp_k, ns_k);
-            std::vector<std::vector<double>> hx(G);
-            for (size_t g = 0; g < G; ++g) {
-                hx[g].resize((size_t)(sws[g]->mx.nt + sws[g]->mx.nc) * 2);
-                xs[g].download(hx[g].data(), hx[g].size());
-            }
-            // towed drag of the members on the axis (main.cpp:90-91)
-            std::vector<sqbem_swimmer*> towed;
-            std::vector<size_t> towed_g;
-            for (size_t g = 0; g < G; ++g)
-                if (inst[ids[g]].towed && std::fabs(prep[ids[g]].b) < 1e-12) {
-                    towed.push_back(sws[g].get());
-                    towed_g.push_back(g);
-                }
-            std::vector<std::vector<double>> hf(towed.size());
-            if (!towed.empty()) {
-                const double w6[6] = {0, 0, 1, 0, 0, 0};
-                DevBuf<double> dw(6, bs);
-                dw.upload(w6, 6);
-                std::vector<DevBuf<double>> xt(towed.size());
-                std::vector<const double*> wi;
-                std::vector<double*> xo;
-                for (size_t t = 0; t < towed.size(); ++t) {
-                    xt[t].alloc((size_t)(towed[t]->mx.nt + towed[t]->mx.nc), bs);
-                    wi.push_back(dw.get());
-                    xo.push_back(xt[t].get());
-                }
-                int it2 = 0;
-                double r2 = 0;
-                mixed_solve(towed, true, wi, 1, xo, cx, &it2, &r2);
-                for (size_t t = 0; t < towed.size(); ++t) {
-                    hf[t].resize(xt[t].n);
-                    xt[t].download(hf[t].data(), hf[t].size());
-                }
-            }
-            CUDA_CHECK(cudaStreamSynchronize(bs));
-            for (size_t g = 0; g < G; ++g) {
-                sqbem_swimmer& s = *sws[g];
-                const int nt = s.mx.nt, ns = s.mx.ns, ldx = nt + s.mx.nc;
-                double* res = results + (size_t)ids[g] * SQBEM_RESULT_STRIDE;
-                for (int c = 0; c < 3; ++c) {
-                    res[c] = hx[g][nt + ns + c];
-                    res[3 + c] = hx[g][nt + ns + 3 + c];
-                    res[6 + c] = hx[g][ldx + nt + ns + c];
-                    res[9 + c] = hx[g][ldx + nt + ns + 3 + c];
-                }
-                res[12] = NAN;
-                res[13] = s.Nt;
-                res[14] = s.Ns;
-                res[15] = iters;
-            }
-            for (size_t t = 0; t < towed.size(); ++t) {
-                sqbem_swimmer& s = *towed[t];
-                double Fz = 0;
-                for (int p = 0; p < s.Ns; ++p) Fz = Fz - s.host_panels[p].area * hf[t][s.mx.nt + 3 * p + 2];
-                results[(size_t)ids[towed_g[t]] * SQBEM_RESULT_STRIDE + 12] = -Fz / (6 * bem::PI);
-            }
-        }
+        const size_t gm = (size_t)group_max();
+        for (size_t c0 = 0; c0 < all.size(); c0 += gm)
+            chunks.push_back({std::vector<int>(all.begin() + c0, all.begin() + std::min(all.size(), c0 + gm)),
+                              std::get<1>(kv.first), std::get<2>(kv.first)});
     }
+    std::stable_sort(chunks.begin(), chunks.end(), [](const Chunk& a, const Chunk& b) {
+        return a.ns != b.ns ? a.ns > b.ns : a.ids.size() > b.ids.size();
+    });
+    const int W = std::min<int>(stream_count(), (int)chunks.size());
+    MemBudget budget(device_budget());
+    int dev = 0;
+    CUDA_CHECK(cudaGetDevice(&dev));
+    cudaEvent_t start;
+    CUDA_CHECK(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    CUDA_CHECK(cudaEventRecord(start, bs));
+    std::atomic<size_t> next{0};
+    std::atomic<bool> failed{false};
+    std::exception_ptr first_error;
+    std::mutex emu;
+    auto worker = [&]() {
+        try {
+            CUDA_CHECK(cudaSetDevice(dev));
+            Stream ws;
+            CUDA_CHECK(cudaStreamWaitEvent(ws, start, 0));
+            PhaseClock pc;
+            for (;;) {
+                const size_t k = next.fetch_add(1);
+                if (k >= chunks.size() || failed.load()) break;
+                const double need = chunk_bytes(chunks[k].ids.size(), chunks[k].ntp, chunks[k].ns);
+                budget.acquire(need);
+                try {
+                    run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, ws, results, pc);
+                    CUDA_CHECK(cudaStreamSynchronize(ws));  // its memory is back in the pool
+                } catch (...) {
+                    budget.release(need);
+                    throw;
+                }
+                budget.release(need);
+            }
+            cudaEvent_t done;
+            CUDA_CHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+            CUDA_CHECK(cudaEventRecord(done, ws));
+            CUDA_CHECK(cudaStreamWaitEvent(bs, done, 0));
+            CUDA_CHECK(cudaEventDestroy(done));
+        } catch (...) {
+            failed.store(true);
+            std::lock_guard<std::mutex> lk(emu);
+            if (!first_error) first_error = std::current_exception();
+        }
+    };
+    if (W <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> th;
+        for (int w = 0; w < W; ++w) th.emplace_back(worker);
+        for (auto& t : th) t.join();
+    }
+    cudaEventDestroy(start);
+    if (first_error) std::rethrow_exception(first_error);
 }
 
 }  // namespace

@@ -26,11 +26,15 @@ constexpr int MAX_DEV = 64;
 cudaMemPool_t g_pools[MAX_DEV] = {};
 std::once_flag g_pool_once[MAX_DEV];
 
+// A block is free, being filled (taken, its copy not yet enqueued) or in
+// flight (its event recorded after the copy); only an in-flight block whose
+// event has completed becomes free again.
+enum class PinState { Free, Filling, InFlight };
 struct Pinned {
     void* p = nullptr;
     size_t bytes = 0;
     cudaEvent_t ev = nullptr;
-    bool busy = false;
+    PinState state = PinState::Free;
 };
 std::mutex g_pin_mu;
 std::deque<Pinned> g_pinned;  // deque: references stay valid as it grows
@@ -66,8 +70,8 @@ void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st) {
     {
         std::lock_guard<std::mutex> lk(g_pin_mu);
         for (Pinned& b : g_pinned) {
-            if (b.busy && cudaEventQuery(b.ev) == cudaSuccess) b.busy = false;
-            if (!b.busy && b.bytes >= bytes && (!blk || b.bytes < blk->bytes)) blk = &b;
+            if (b.state == PinState::InFlight && cudaEventQuery(b.ev) == cudaSuccess) b.state = PinState::Free;
+            if (b.state == PinState::Free && b.bytes >= bytes && (!blk || b.bytes < blk->bytes)) blk = &b;
         }
         if (!blk && g_pinned_total + bytes <= PINNED_CAP) {
             Pinned b;
@@ -83,15 +87,20 @@ void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st) {
                 (void)cudaGetLastError();
             }
         }
-        if (blk) blk->busy = true;
+        if (blk) blk->state = PinState::Filling;
     }
     if (!blk) {  // staging full: the plain copy is still correct
         CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
         return;
     }
     std::memcpy(blk->p, src, bytes);
-    CUDA_CHECK(cudaMemcpyAsync(dst, blk->p, bytes, cudaMemcpyHostToDevice, st));
-    CUDA_CHECK(cudaEventRecord(blk->ev, st));
+    const cudaError_t e1 = cudaMemcpyAsync(dst, blk->p, bytes, cudaMemcpyHostToDevice, st);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaEventRecord(blk->ev, st) : e1;
+    {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        blk->state = e2 == cudaSuccess ? PinState::InFlight : PinState::Free;
+    }
+    CUDA_CHECK(e2);
 }
 
 }  // namespace sqbem

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -217,11 +218,10 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
 constexpr int DIAG_SMEM = (3 * MX_NB * DP + MX_NB) * (int)sizeof(float);
 
 void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         CUDA_CHECK(cudaFuncSetAttribute(diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM));
-        attr = true;
-    }
+    });
     for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
         DiagArgs a;
         a.flag = cx.flag;

@@ -453,6 +453,7 @@ CUtensorMap make_map(const bf16* base, int rows, int k, long long ld) {
 }
 
 int g_num_sms = 0;
+std::once_flag g_sms_once;
 
 }  // namespace
 
@@ -467,12 +468,12 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
              cudaStream_t st) {
     if (probs_in.size() != ops.size()) fail(SQBEM_ERR_ARG, "tc_gemm: operand count");
     get_encode();
-    if (!g_num_sms) {
+    std::call_once(g_sms_once, [] {
         int dev = 0;
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
         CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    }
+    });
     KArgs a;
     auto h0 = std::chrono::steady_clock::now();
     auto flush = [&](double flops, double bytes) {

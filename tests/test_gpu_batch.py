@@ -62,3 +62,20 @@ def test_batch_rejects_bad_instances():
         sqbem.kinematics_batch([dict(a_over_R=1.5, beta=0.0, sphere_level=2)], sqbem.MIXED)
     with pytest.raises(sqbem.BEMError):
         sqbem.kinematics_batch([dict(a_over_R=0.3, beta=0.0, sphere_level=2, e=(0, 0, 2.0))], sqbem.MIXED)
+
+
+def test_concurrent_chunks_match_sequential(monkeypatch):
+    """groups run on several host threads / streams (SQBEM_STREAMS): the results
+    are bitwise those of one stream (no shared scratch between the chunks)"""
+    rng = np.random.default_rng(21)
+    insts = []
+    for k in range(10):
+        insts.append(dict(a_over_R=float(rng.uniform(0.2, 0.5)), beta=float(rng.uniform(0, 0.4)), L_over_R=4.0,
+                          e=(0.0, 0.0, 1.0), n_theta=int(rng.choice([10, 12, 14])), n_r=3,
+                          sphere_level=int(rng.choice([1, 2])), towed=0))
+    monkeypatch.setenv("SQBEM_STREAMS", "1")
+    r1, _ = sqbem.kinematics_batch(insts, sqbem.MIXED)
+    monkeypatch.setenv("SQBEM_STREAMS", "3")
+    for _ in range(2):
+        r3, _ = sqbem.kinematics_batch(insts, sqbem.MIXED)
+        np.testing.assert_array_equal(r3[:, :12], r1[:, :12])
