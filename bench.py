@@ -304,7 +304,7 @@ def main():
                                   "launch's duration includes the kernels of other streams sharing the GPU")
     # the same classes from one extra, untimed step on a single stream: the
     # kernels' own rates, without co-scheduling
-    roofline_1s = None
+    roofline_1s, st1 = None, None
     if rank == 0 and args.impl == "gb300":
         prev = os.environ.get("SQBEM_STREAMS")
         os.environ["SQBEM_STREAMS"] = "1"
@@ -320,11 +320,13 @@ def main():
     # assembly throughput: far-kernel flops are credited at 7 x FLOPS_PER_EVAL (= 64,
     # csrc/assemble.cuh) per (target, panel) pair
     assembly = None
-    if "assemble_far" in stats:
-        _, s_far, f_far, b_far = stats["assemble_far"]
-        s_near = stats.get("assemble_near", (0, 0.0, 0.0, 0.0))[1]
+    kst = st1 if roofline_1s is not None else stats  # kernel durations without co-scheduling
+    if "assemble_far" in kst:
+        _, s_far, f_far, b_far = kst["assemble_far"]
+        s_near = kst.get("assemble_near", (0, 0.0, 0.0, 0.0))[1]
         pairs = f_far / (7 * 64)
-        assembly = {"panel_pairs_per_step": pairs / args.steps, "pairs_per_s": pairs / (s_far + s_near),
+        steps_in = 1 if roofline_1s is not None else args.steps
+        assembly = {"panel_pairs_per_step": pairs / steps_in, "pairs_per_s": pairs / (s_far + s_near),
                     "far_kernel_written_gbs": b_far / s_far / 1e9,
                     "far_kernel_frac_of_hbm": b_far / s_far / 1e9 / peaks["hbm_gbs"],
                     "seconds_far_near": [s_far, s_near]}
