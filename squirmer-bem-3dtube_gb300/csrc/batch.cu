@@ -307,29 +307,13 @@ double device_budget() {
     return 0.8 * ((double)fr + (double)(reserved > in_use ? reserved - in_use : 0));
 }
 
-void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
-               double* results) {
-    std::map<std::tuple<int, int, int>, std::vector<int>> groups;
-    for (int k = 0; k < n; ++k) {
-        const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
-        groups[{prep[k].bounded ? 1 : 0, ntp, prep[k].sphere.P()}].push_back(k);
-    }
-    struct Chunk {
-        std::vector<int> ids;
-        int ntp, ns;
-    };
-    std::vector<Chunk> chunks;
-    for (auto& kv : groups) {
-        const std::vector<int>& all = kv.second;
-        const size_t gm = (size_t)group_max();
-        for (size_t c0 = 0; c0 < all.size(); c0 += gm)
-            chunks.push_back({std::vector<int>(all.begin() + c0, all.begin() + std::min(all.size(), c0 + gm)),
-                              std::get<1>(kv.first), std::get<2>(kv.first)});
-    }
-    std::stable_sort(chunks.begin(), chunks.end(), [](const Chunk& a, const Chunk& b) {
-        return a.ns != b.ns ? a.ns > b.ns : a.ids.size() > b.ids.size();
-    });
-    const int W = std::min<int>(stream_count(), (int)chunks.size());
+// Runs work(k, stream) for k < ntasks on up to stream_count() host threads, each
+// with its own stream, tasks taken in order from a shared counter, every task's
+// estimated device bytes held against the memory budget while it runs.  Events
+// make the batch stream bs cover all of it.  The first failure is rethrown.
+template <class Work>
+void run_concurrent(size_t ntasks, const std::vector<double>& task_bytes, cudaStream_t bs, Work&& work) {
+    const int W = std::min<int>(stream_count(), (int)ntasks);
     MemBudget budget(device_budget());
     int dev = 0;
     CUDA_CHECK(cudaGetDevice(&dev));
@@ -345,20 +329,18 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
             CUDA_CHECK(cudaSetDevice(dev));
             Stream ws;
             CUDA_CHECK(cudaStreamWaitEvent(ws, start, 0));
-            PhaseClock pc;
             for (;;) {
                 const size_t k = next.fetch_add(1);
-                if (k >= chunks.size() || failed.load()) break;
-                const double need = chunk_bytes(chunks[k].ids.size(), chunks[k].ntp, chunks[k].ns);
-                budget.acquire(need);
+                if (k >= ntasks || failed.load()) break;
+                budget.acquire(task_bytes[k]);
                 try {
-                    run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, ws, results, pc);
+                    work(k, (cudaStream_t)ws);
                     CUDA_CHECK(cudaStreamSynchronize(ws));  // its memory is back in the pool
                 } catch (...) {
-                    budget.release(need);
+                    budget.release(task_bytes[k]);
                     throw;
                 }
-                budget.release(need);
+                budget.release(task_bytes[k]);
             }
             cudaEvent_t done;
             CUDA_CHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
@@ -382,6 +364,55 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
     if (first_error) std::rethrow_exception(first_error);
 }
 
+void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
+               double* results) {
+    std::map<std::tuple<int, int, int>, std::vector<int>> groups;
+    for (int k = 0; k < n; ++k) {
+        const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
+        groups[{prep[k].bounded ? 1 : 0, ntp, prep[k].sphere.P()}].push_back(k);
+    }
+    struct Chunk {
+        std::vector<int> ids;
+        int ntp, ns;
+    };
+    std::vector<Chunk> chunks;
+    for (auto& kv : groups) {
+        const std::vector<int>& all = kv.second;
+        const size_t gm = (size_t)group_max();
+        for (size_t c0 = 0; c0 < all.size(); c0 += gm)
+            chunks.push_back({std::vector<int>(all.begin() + c0, all.begin() + std::min(all.size(), c0 + gm)),
+                              std::get<1>(kv.first), std::get<2>(kv.first)});
+    }
+    // the larger spheres first: the longest tasks start early
+    std::stable_sort(chunks.begin(), chunks.end(), [](const Chunk& a, const Chunk& b) {
+        return a.ns != b.ns ? a.ns > b.ns : a.ids.size() > b.ids.size();
+    });
+    std::vector<double> bytes;
+    for (const Chunk& c : chunks) bytes.push_back(chunk_bytes(c.ids.size(), c.ntp, c.ns));
+    run_concurrent(chunks.size(), bytes, bs, [&](size_t k, cudaStream_t st) {
+        PhaseClock pc;
+        run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, results, pc);
+    });
+}
+
+// FP64: one instance per task, the same concurrency as the mixed path.
+void run_fp64(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
+              double* results) {
+    std::vector<int> order(n);
+    for (int k = 0; k < n; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return prep[a].sphere.P() > prep[b].sphere.P(); });
+    std::vector<double> bytes;
+    for (int k : order) {
+        const double t = 3.0 * (prep[k].bounded ? prep[k].tube.P() : 0), s = 3.0 * prep[k].sphere.P();
+        bytes.push_back(1.25 * 8.0 * (3.0 * t * t + 6.0 * t * s + 6.0 * s * s));
+    }
+    run_concurrent((size_t)n, bytes, bs, [&](size_t j, cudaStream_t st) {
+        const int k = order[j];
+        run_one(inst[k], prep[k], SQBEM_FP64, st, results + (size_t)k * SQBEM_RESULT_STRIDE);
+    });
+}
+
 }  // namespace
 
 extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
@@ -400,9 +431,7 @@ extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int pre
         EventTimer clk;
         clk.start(bs);
         if (precision == SQBEM_MIXED) run_mixed(n, inst, prep, bs, results);
-        else
-            for (int k = 0; k < n; ++k)
-                run_one(inst[k], prep[k], precision, bs, results + (size_t)k * SQBEM_RESULT_STRIDE);
+        else run_fp64(n, inst, prep, bs, results);
         clk.stop(bs);
         const double secs = clk.seconds();
         if (device_seconds) *device_seconds = secs;

@@ -73,9 +73,10 @@ def test_concurrent_chunks_match_sequential(monkeypatch):
         insts.append(dict(a_over_R=float(rng.uniform(0.2, 0.5)), beta=float(rng.uniform(0, 0.4)), L_over_R=4.0,
                           e=(0.0, 0.0, 1.0), n_theta=int(rng.choice([10, 12, 14])), n_r=3,
                           sphere_level=int(rng.choice([1, 2])), towed=0))
-    monkeypatch.setenv("SQBEM_STREAMS", "1")
-    r1, _ = sqbem.kinematics_batch(insts, sqbem.MIXED)
-    monkeypatch.setenv("SQBEM_STREAMS", "3")
-    for _ in range(2):
-        r3, _ = sqbem.kinematics_batch(insts, sqbem.MIXED)
-        np.testing.assert_array_equal(r3[:, :12], r1[:, :12])
+    for prec in (sqbem.MIXED, sqbem.FP64):
+        monkeypatch.setenv("SQBEM_STREAMS", "1")
+        r1, _ = sqbem.kinematics_batch(insts, prec)
+        monkeypatch.setenv("SQBEM_STREAMS", "3")
+        for _ in range(2):
+            r3, _ = sqbem.kinematics_batch(insts, prec)
+            np.testing.assert_array_equal(r3[:, :12], r1[:, :12])
