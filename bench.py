@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "kinematics"])
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "kinematics", "ensemble", "adjoint"],
+                    help="sweep (the headline) / kinematics: kinematics_batch; ensemble: 256 swimmers, RK4 "
+                         "(plus the 25x25x41 field); adjoint: the 32-instance adjoint batch")
     ap.add_argument("--instances", type=int, default=0,
                     help="first N instances of the workload only (small cases for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -248,9 +250,83 @@ def run_reference(args, rank, ws, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_aux(args, rank, ws):
+    """Secondary workloads (configs 4 and 5), one JSON line each; not the headline."""
+    import math
+    import numpy as np
+    import sqbem
+    from sqbem import workloads
+    prec = sqbem.MIXED if args.precision == "mixed" else sqbem.FP64
+    clocks = Clocks()
+    if args.workload == "ensemble":
+        w = workloads.ensemble()
+        if args.instances:
+            w = w[:args.instances]
+        R = 1.0 / w[0]["a_over_R"]
+        y0 = np.array([[d["beta0"] * (R - 1.0), 0.0, 0.0, *d["e"]] for d in w])
+        alpha = np.array([d["alpha"] for d in w])
+        P = sqbem.TrajParams(a_over_R=w[0]["a_over_R"], dt=w[0]["dt"], n_theta=w[0]["n_theta"],
+                             sphere_level=w[0]["sphere_level"], L_over_R=w[0]["L_over_R"])
+        rk_steps = 2  # RK4 steps per bench step (4 evaluations each)
+        for _ in range(args.warmup):
+            sqbem.trajectory_ensemble(y0, alpha, P, rk_steps, scheme=1, precision=prec)
+        clocks.start()
+        gpu_s, wall0, solves, states = 0.0, time.perf_counter(), 0, None
+        for _ in range(args.steps):
+            states, U, Om, status, secs = sqbem.trajectory_ensemble(y0, alpha, P, rk_steps, scheme=1, precision=prec)
+            gpu_s += secs
+            solves += 4 * rk_steps * len(w)
+        wall = time.perf_counter() - wall0
+        clk = clocks.stop()
+        u, fsecs = sqbem.ensemble_field(states[:, -1, :], alpha, P, 25, 25, 41, 7.0, precision=prec)
+        pts = int(np.sum(~np.isnan(u[..., 0])))
+        line = {"metric": "trajectory-ensemble BEM solves/sec (each solve: swimmer re-assembly, Schur and the two "
+                          "slip modes against the shared tube inverse)", "value": solves / gpu_s, "unit": "solves/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * gpu_s / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32/bf16x3+f64" if prec == sqbem.MIXED else "f64", "data": "synthetic",
+                "config": {"workload": "ensemble (%d swimmers, a/R = %.1f, level %d, n_theta = %d, RK4 dt = %g, "
+                                       "%d steps per call; the tube factored once per call)"
+                                       % (len(w), w[0]["a_over_R"], w[0]["sphere_level"], w[0]["n_theta"], w[0]["dt"],
+                                          rk_steps)},
+                "e2e": {"value": solves / wall, "unit": "solves/s"},
+                "field": {"grid": [25, 25, 41], "points_evaluated": pts, "seconds": fsecs,
+                          "points_per_s": pts / fsecs,
+                          "note": "the field call re-solves every swimmer at its final state, then evaluates"},
+                "clocks": clk}
+    else:  # adjoint
+        insts = workloads.adjoint()
+        for _ in range(args.warmup):
+            sqbem.adjoint_batch(insts[:4])
+        clocks.start()
+        gpu_s, wall0 = 0.0, time.perf_counter()
+        for _ in range(args.steps):
+            res, secs = sqbem.adjoint_batch(insts)
+            gpu_s += secs
+        wall = time.perf_counter() - wall0
+        clk = clocks.stop()
+        n = len(insts) * args.steps
+        line = {"metric": "adjoint evaluations/sec (U, Omega and d(U, Omega)/dc for both slip modes, FP64)",
+                "value": n / gpu_s, "unit": "instances/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * gpu_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "adjoint (32 instances, level 2, n_theta = 24)"},
+                "e2e": {"value": n / wall, "unit": "instances/s"}, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, ws, dist = dist_init(args.gpus)
+    if args.workload in ("ensemble", "adjoint"):
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the sweep and "
+                                  "kinematics workloads only"}), flush=True)
+            return
+        run_aux(args, rank, ws)
+        return
     if args.impl == "reference":
         run_reference(args, rank, ws, dist)
         return

@@ -20,6 +20,7 @@
 
 #include "bem/utils/mesh.hpp"
 #include "common.cuh"
+#include "concurrent.cuh"
 #include "solver.cuh"
 
 using namespace sqbem;
@@ -253,115 +254,12 @@ void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_ins
     }
 }
 
-// Chunks run concurrently: SQBEM_STREAMS host threads (default 2), each with
-// its own stream, take chunks from a shared queue (the larger spheres first),
-// so that one chunk's latency-bound phases (diagonal LU leaves, small
-// updates, host synchronisations) overlap another's large GEMMs.  The batch
-// stream's events bracket all of them.
-int stream_count() {
-    const char* e = std::getenv("SQBEM_STREAMS");
-    const int v = e ? std::atoi(e) : 6;
-    return std::max(1, std::min(v, 8));
-}
-
 // Device bytes a chunk holds at its peak, estimated from its sizes (FP32 tube
 // block, inverse and split copies; swimmer blocks B, A_uBt, D, E, A_uBs, Y,
 // G_s^{-1}; the LU working set), with a margin.
 double chunk_bytes(size_t G, int ntp, int ns) {
     const double t = ntp, s = pad128(3 * ns);
     return 1.25 * G * 4.0 * (6.0 * t * t + 6.0 * t * s + 5.0 * s * s);
-}
-
-// Concurrent chunks share a memory budget: free device memory plus what the
-// library's pool holds unused, times 0.8.  A chunk waits while its estimate
-// does not fit next to the running ones (one chunk always runs).
-class MemBudget {
-public:
-    explicit MemBudget(double budget) : budget_(budget) {}
-    void acquire(double b) {
-        std::unique_lock<std::mutex> lk(mu_);
-        cv_.wait(lk, [&] { return used_ == 0 || used_ + b <= budget_; });
-        used_ += b;
-    }
-    void release(double b) {
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            used_ -= b;
-        }
-        cv_.notify_all();
-    }
-
-private:
-    std::mutex mu_;
-    std::condition_variable cv_;
-    double budget_, used_ = 0;
-};
-
-double device_budget() {
-    size_t fr = 0, tot = 0;
-    CUDA_CHECK(cudaMemGetInfo(&fr, &tot));
-    cuuint64_t reserved = 0, in_use = 0;
-    cudaMemPool_t pool = device_pool();
-    CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
-    CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &in_use));
-    return 0.8 * ((double)fr + (double)(reserved > in_use ? reserved - in_use : 0));
-}
-
-// Runs work(k, stream) for k < ntasks on up to stream_count() host threads, each
-// with its own stream, tasks taken in order from a shared counter, every task's
-// estimated device bytes held against the memory budget while it runs.  Events
-// make the batch stream bs cover all of it.  The first failure is rethrown.
-template <class Work>
-void run_concurrent(size_t ntasks, const std::vector<double>& task_bytes, cudaStream_t bs, Work&& work) {
-    const int W = std::min<int>(stream_count(), (int)ntasks);
-    MemBudget budget(device_budget());
-    int dev = 0;
-    CUDA_CHECK(cudaGetDevice(&dev));
-    cudaEvent_t start;
-    CUDA_CHECK(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-    CUDA_CHECK(cudaEventRecord(start, bs));
-    std::atomic<size_t> next{0};
-    std::atomic<bool> failed{false};
-    std::exception_ptr first_error;
-    std::mutex emu;
-    auto worker = [&]() {
-        try {
-            CUDA_CHECK(cudaSetDevice(dev));
-            Stream ws;
-            CUDA_CHECK(cudaStreamWaitEvent(ws, start, 0));
-            for (;;) {
-                const size_t k = next.fetch_add(1);
-                if (k >= ntasks || failed.load()) break;
-                budget.acquire(task_bytes[k]);
-                try {
-                    work(k, (cudaStream_t)ws);
-                    CUDA_CHECK(cudaStreamSynchronize(ws));  // its memory is back in the pool
-                } catch (...) {
-                    budget.release(task_bytes[k]);
-                    throw;
-                }
-                budget.release(task_bytes[k]);
-            }
-            cudaEvent_t done;
-            CUDA_CHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
-            CUDA_CHECK(cudaEventRecord(done, ws));
-            CUDA_CHECK(cudaStreamWaitEvent(bs, done, 0));
-            CUDA_CHECK(cudaEventDestroy(done));
-        } catch (...) {
-            failed.store(true);
-            std::lock_guard<std::mutex> lk(emu);
-            if (!first_error) first_error = std::current_exception();
-        }
-    };
-    if (W <= 1) {
-        worker();
-    } else {
-        std::vector<std::thread> th;
-        for (int w = 0; w < W; ++w) th.emplace_back(worker);
-        for (auto& t : th) t.join();
-    }
-    cudaEventDestroy(start);
-    if (first_error) std::rethrow_exception(first_error);
 }
 
 void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
@@ -452,19 +350,28 @@ extern "C" int sqbem_adjoint_batch(int n, const sqbem_instance* inst, int precis
         Stream bs;
         EventTimer clk;
         clk.start(bs);
+        std::vector<Prepared> prep;
+        prep.reserve(n);
+        for (int k = 0; k < n; ++k) prep.push_back(prepare(inst[k]));
+        std::vector<double> bytes;
         for (int k = 0; k < n; ++k) {
-            const Prepared P = prepare(inst[k]);
+            const double t = 3.0 * (prep[k].bounded ? prep[k].tube.P() : 0), sp = 3.0 * prep[k].sphere.P();
+            bytes.push_back(1.25 * 8.0 * (3.0 * t * t + 7.0 * t * sp + 6.0 * sp * sp));
+        }
+        run_concurrent((size_t)n, bytes, bs, [&](size_t kk, cudaStream_t st) {
+            const int k = (int)kk;
+            const Prepared& P = prep[k];
             std::unique_ptr<sqbem_tube> t;
             if (P.bounded) {
                 t = std::make_unique<sqbem_tube>();
-                t->st.borrow(bs);
+                t->st.borrow(st);
                 t->R = P.R; t->L = P.L; t->a = 1.0; t->n_theta = inst[k].n_theta; t->n_r = inst[k].n_r; t->mu = 1.0;
                 t->precision = SQBEM_FP64;
                 t->mesh = P.tube;
                 t->build_device();
             }
             sqbem_swimmer s;
-            s.st.borrow(bs);
+            s.st.borrow(st);
             const double c[3] = {P.b, 0, 0};
             s.build(t.get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_FP64);
             auto slips = squirmer_slip_host(s.host_panels, c, inst[k].e, 1, 0);
@@ -484,7 +391,7 @@ extern "C" int sqbem_adjoint_batch(int n, const sqbem_instance* inst, int precis
                     o[15 + e] = dOm[9 * m + e];
                 }
             }
-        }
+        });
         clk.stop(bs);
         const double secs = clk.seconds();
         if (device_seconds) *device_seconds = secs;

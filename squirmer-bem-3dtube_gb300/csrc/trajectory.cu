@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -23,6 +24,7 @@
 #include "bem/utils/io.hpp"
 #include "bem/utils/mesh.hpp"
 #include "common.cuh"
+#include "concurrent.cuh"
 #include "solver.cuh"
 
 using namespace sqbem;
@@ -79,7 +81,7 @@ public:
         std::vector<std::array<double, 3>> centre;
     };
 
-    void solve_group(const std::vector<State>& ys, size_t c0, size_t G, bool keep, Group& gr) {
+    void solve_group(const std::vector<State>& ys, size_t c0, size_t G, bool keep, Group& gr, cudaStream_t st) {
         gr.sw.resize(G);
         gr.slips.resize(G);
         gr.modes.resize(G);
@@ -92,7 +94,7 @@ public:
             S.translate({c[0], c[1], c[2]});
             const auto V = mesh_vertices(S);
             gr.sw[g] = std::make_unique<sqbem_swimmer>();
-            gr.sw[g]->st.borrow(tube_->st);
+            gr.sw[g]->st.borrow(st);
             const bem::V3 e = bem::unit(bem::V3{y[3], y[4], y[5]});
             const double ev[3] = {e.x, e.y, e.z};
             if (prec_ == SQBEM_MIXED) {
@@ -107,9 +109,9 @@ public:
         if (prec_ == SQBEM_MIXED) {
             std::vector<sqbem_swimmer*> sp;
             for (auto& s : gr.sw) sp.push_back(s.get());
-            DevBuf<int> flags(2, tube_->st);
+            DevBuf<int> flags(2, st);
             flags.zero();
-            MixedCtx cx{tube_->st, flags.get(), flags.get() + 1};
+            MixedCtx cx{st, flags.get(), flags.get() + 1};
             mixed_build_swimmers(sp, cx);
             std::vector<DevBuf<double>> din(G);
             gr.dx.clear();
@@ -117,9 +119,9 @@ public:
             std::vector<const double*> ip;
             std::vector<double*> xp;
             for (size_t g = 0; g < G; ++g) {
-                din[g].alloc(gr.slips[g].size(), tube_->st);
+                din[g].alloc(gr.slips[g].size(), st);
                 din[g].upload(gr.slips[g].data(), gr.slips[g].size());
-                gr.dx[g].alloc((size_t)(sp[g]->mx.nt + sp[g]->mx.nc) * 2, tube_->st);
+                gr.dx[g].alloc((size_t)(sp[g]->mx.nt + sp[g]->mx.nc) * 2, st);
                 ip.push_back(din[g].get());
                 xp.push_back(gr.dx[g].get());
             }
@@ -132,9 +134,9 @@ public:
                 std::vector<double> w(12);
                 for (int k = 0; k < 2; ++k)
                     CUDA_CHECK(cudaMemcpyAsync(w.data() + 6 * k, gr.dx[g].get() + k * ld + M.nt + M.ns,
-                                               6 * sizeof(double), cudaMemcpyDeviceToHost, tube_->st));
+                                               6 * sizeof(double), cudaMemcpyDeviceToHost, st));
                 count_d2h(12 * sizeof(double));
-                CUDA_CHECK(cudaStreamSynchronize(tube_->st));
+                CUDA_CHECK(cudaStreamSynchronize(st));
                 Modes& m = gr.modes[g];
                 for (int q = 0; q < 3; ++q) {
                     m.U1[q] = w[q]; m.O1[q] = w[3 + q]; m.U2[q] = w[6 + q]; m.O2[q] = w[9 + q];
@@ -161,42 +163,55 @@ public:
                 }
             }
         }
-        evals_ += G;
+        evals_.fetch_add((long long)G);
     }
 
+    // per-group device bytes (swimmer blocks B, A_uBt, D, Y, E, A_uBs, G_s^{-1}), with a margin
+    double group_bytes(size_t G) const {
+        const double t = 3.0 * tube_->Nt, sph = 3.0 * sph0_.P();
+        return 1.25 * G * 4.0 * (6.0 * t * sph + 5.0 * sph * sph + 2.0 * t);
+    }
+
+    // The groups of an evaluation are independent: they run concurrently
+    // (concurrent.cuh), each on its own stream, sharing the tube's factors.
     std::vector<Modes> modes(const std::vector<State>& ys) {
         std::vector<Modes> out(ys.size());
-        for (size_t c0 = 0; c0 < ys.size(); c0 += TRAJ_GROUP) {
-            const size_t G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
+        const size_t ntask = (ys.size() + TRAJ_GROUP - 1) / TRAJ_GROUP;
+        std::vector<double> bytes;
+        for (size_t k = 0; k < ntask; ++k) bytes.push_back(group_bytes(std::min<size_t>(TRAJ_GROUP, ys.size() - k * TRAJ_GROUP)));
+        run_concurrent(ntask, bytes, tube_->st, [&](size_t k, cudaStream_t st) {
+            const size_t c0 = k * TRAJ_GROUP, G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
             Group gr;
-            solve_group(ys, c0, G, false, gr);
+            solve_group(ys, c0, G, false, gr, st);
             for (size_t g = 0; g < G; ++g) out[c0 + g] = gr.modes[g];
-        }
+        });
         return out;
     }
 
     // Lab-frame velocity (swimmer.hpp:163-173, field.hpp:18-34) of swimmer k
     // (B1 = 1, B2 = alpha[k]) at the unmasked points of its grid.
     void fields(const std::vector<State>& ys, const double* alpha, const GridSpec& gs, double* u_out);
-    long long evals() const { return evals_; }
+    long long evals() const { return evals_.load(); }
 
 private:
     int prec_;
     double a_ = 1, R_ = 1;
     std::unique_ptr<sqbem_tube> tube_;
     bem::Mesh sph0_;
-    long long evals_ = 0;
+    std::atomic<long long> evals_{0};
 };
 
 void Evaluator::fields(const std::vector<State>& ys, const double* alpha, const GridSpec& gs, double* u_out) {
     const int Nt = tube_->Nt;
     const size_t npg = (size_t)gs.nx * gs.ny * gs.nz;
     const double lim = 0.97 * R_;
-    cudaStream_t st = tube_->st;
-    for (size_t c0 = 0; c0 < ys.size(); c0 += TRAJ_GROUP) {
-        const size_t G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
+    const size_t ntask = (ys.size() + TRAJ_GROUP - 1) / TRAJ_GROUP;
+    std::vector<double> bytes;
+    for (size_t k = 0; k < ntask; ++k) bytes.push_back(group_bytes(std::min<size_t>(TRAJ_GROUP, ys.size() - k * TRAJ_GROUP)));
+    run_concurrent(ntask, bytes, tube_->st, [&](size_t task, cudaStream_t st) {
+        const size_t c0 = task * TRAJ_GROUP, G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
         Group gr;
-        solve_group(ys, c0, G, true, gr);
+        solve_group(ys, c0, G, true, gr, st);
         for (size_t g = 0; g < G; ++g) {
             const size_t k = c0 + g;
             sqbem_swimmer& s = *gr.sw[g];
@@ -283,7 +298,7 @@ void Evaluator::fields(const std::vector<State>& ys, const double* alpha, const 
             for (int q = 0; q < npts; ++q)
                 for (int d = 0; d < 3; ++d) uk[3 * idx[q] + d] = ho[3 * (size_t)q + d];
         }
-    }
+    });
 }
 
 // state derivative (trajectory.hpp:52-65): U = U1 + alpha U2, de/dt = Omega x e
