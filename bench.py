@@ -452,6 +452,8 @@ def main():
         "cpu_baseline": cpu,
         "kernel_stats": {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]}
                          for c, v in stats.items()},
+        "kernel_stats_single_stream": None if st1 is None else
+        {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]} for c, v in st1.items()},
     }
     print(json.dumps(line), flush=True)
 

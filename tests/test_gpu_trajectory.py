@@ -209,3 +209,20 @@ def test_ensemble_field_mixed_vs_fp64():
     err = np.max(np.abs(umx[ok] - u64[ok])) / np.max(np.abs(u64[ok]))
     print("mixed field rel err", err)
     assert err < 2e-5, err
+
+
+def test_ensemble_streams_do_not_change_results(monkeypatch):
+    """100 swimmers = 3 groups of at most 48, solved concurrently on several
+    streams: bitwise the single-stream trajectories and field"""
+    P = sqbem.TrajParams(a_over_R=0.3, dt=0.25, n_theta=8, sphere_level=1)
+    rng = np.random.default_rng(31)
+    y0 = _initial_states(P, 100, rng)
+    alpha = rng.uniform(-4, 4, 100)
+    out = {}
+    for ns in ("1", "4"):
+        monkeypatch.setenv("SQBEM_STREAMS", ns)
+        s, U, Om, st, _ = sqbem.trajectory_ensemble(y0, alpha, P, 2, scheme=1, precision=sqbem.MIXED)
+        u, _ = sqbem.ensemble_field(s[:, -1, :], alpha, P, 5, 5, 7, 4.0, precision=sqbem.MIXED)
+        out[ns] = (s, U, u)
+    for a, b in zip(out["1"], out["4"]):
+        np.testing.assert_array_equal(a, b)
