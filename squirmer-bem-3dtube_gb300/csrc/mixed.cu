@@ -87,9 +87,9 @@ __device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x
 // shared memory (with both inverses: 3 x 128 x 129 floats).
 //
 // LU, blocked right-looking with 16-column panels:
-//   panel   4 threads per row, each 4 of the panel's columns; one barrier per
-//           column (the multiplier is read by the row's 4 threads, which share a
-//           warp, before the one owning the pivot column overwrites it);
+//   panel   warps 0-3, a thread per row held in registers, a named barrier of
+//           those 128 threads per column (one warp alone is latency-bound; a
+//           CTA-wide barrier per column costs more than the arithmetic);
 //   U12     one thread per column solves with the unit-lower 16 x 16 block;
 //   A22     rank-16 update, 4 rows x 1 column per thread (columns across the
 //           warp: conflict-free; the row values are broadcasts).
@@ -119,28 +119,35 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     }
     __syncthreads();
     int bad = 0;
-    const int pi = tid >> 2, pg = tid & 3;  // panel step: row, quarter of the panel
     for (int c0 = 0; c0 < N; c0 += DG_PW) {
-        for (int j = c0; j < c0 + DG_PW; ++j) {
-            const float piv = a[j][j];
-            if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
-            const bool act = pi > j;
-            const float l = act ? a[pi][j] / piv : 0.f;
-            __syncwarp();
-            if (act) {
+        if (tid < 128) {
+            // the panel, by warps 0-3: thread t owns row j + 1 + t, kept in registers
+            // with compile-time column indices; the four warps meet at a named
+            // barrier per column (the other warps wait at the CTA barrier below)
+            for (int jj = 0; jj < DG_PW; ++jj) {
+                const int j = c0 + jj;
+                const float piv = a[j][j];
+                if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+                const int i = j + 1 + tid;
+                if (i < N) {
+                    float prow[DG_PW], row[DG_PW];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int c = c0 + 4 * pg + q;
-                    if (c > j) {
-                        a[pi][c] = fmaf(-l, a[j][c], a[pi][c]);
-                    } else if (c == j) {
-                        a[pi][c] = l;
-                        if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+                    for (int cc = 0; cc < DG_PW; ++cc) {
+                        prow[cc] = a[j][c0 + cc];
+                        row[cc] = a[i][c0 + cc];
+                    }
+                    const float l = a[i][j] / piv;
+                    if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+#pragma unroll
+                    for (int cc = 0; cc < DG_PW; ++cc) {
+                        if (cc > jj) a[i][c0 + cc] = fmaf(-l, prow[cc], row[cc]);
+                        else if (cc == jj) a[i][c0 + cc] = l;
                     }
                 }
+                asm volatile("bar.sync 1, 128;" ::: "memory");
             }
-            __syncthreads();
         }
+        __syncthreads();
         {  // U12 = L11^{-1} A12
             const int c = c0 + DG_PW + tid;
             if (c < N)
@@ -294,7 +301,9 @@ void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool low
             p.C = t.X + k0 + (long long)j0 * t.ldx; p.c_rs = 1; p.c_cs = t.ldx;
             p.O_hi = t.Ch + k0 + (long long)j0 * t.ldc; p.O_lo = t.Cl + k0 + (long long)j0 * t.ldc;
             p.o_rs = 1; p.o_cs = t.ldc;
-            if (t.Rh) {
+            // the row-major copy; an inversion's lower solve skips it (the upper
+            // solve rewrites every row)
+            if (t.Rh && !(tri && lower)) {
                 p.P_hi = t.Rh + (long long)k0 * t.ldr + j0; p.P_lo = t.Rl + (long long)k0 * t.ldr + j0;
                 p.p_rs = t.ldr; p.p_cs = 1;
             }
