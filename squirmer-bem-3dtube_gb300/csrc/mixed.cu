@@ -87,15 +87,15 @@ __device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x
 // shared memory (with both inverses: 3 x 128 x 129 floats).
 //
 // LU, blocked right-looking with 16-column panels:
-//   panel   warps 0-3, a thread per row held in registers, a named barrier of
-//           those 128 threads per column (one warp alone is latency-bound; a
-//           CTA-wide barrier per column costs more than the arithmetic);
+//   panel   warps 0-3, each thread holding one row of the panel in registers
+//           for all 16 columns; the pivot row is broadcast through a
+//           double-buffered shared copy, one named barrier of those 128 threads
+//           per column (one warp alone is latency-bound; a CTA-wide barrier
+//           per column costs more than the arithmetic);
 //   U12     one thread per column solves with the unit-lower 16 x 16 block;
 //   A22     rank-16 update, 4 rows x 1 column per thread (columns across the
 //           warp: conflict-free; the row values are broadcasts).
-// Inverses: threads 0-255 form L^{-1} and 256-511 U^{-1}, two threads per
-// column splitting each inner sum (combined with a shuffle); only the nonzero
-// triangle of every column is visited.
+// Inverses: blocked by 16 with 4 x 4 register tiles (see below).
 struct DiagArgs {
     int* flag;
     DiagJob j[MAXJOBS];
@@ -110,6 +110,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     float(*xl)[DP] = reinterpret_cast<float(*)[DP]>(sh + N * DP);
     float(*xu)[DP] = reinterpret_cast<float(*)[DP]>(sh + 2 * N * DP);
     float* rd = sh + 3 * N * DP;  // 1 / U(r, r)
+    float(*tl)[DP] = reinterpret_cast<float(*)[DP]>(sh + 3 * N * DP + N);            // 16 x N scratch (L^{-1})
+    float(*tu)[DP] = reinterpret_cast<float(*)[DP]>(sh + 3 * N * DP + N + DG_PW * DP);  // 16 x N scratch (U^{-1})
+    __shared__ float prow_buf[2][DG_PW];  // the panel's pivot row, double-buffered
     const DiagJob& J = args.j[blockIdx.x];
     const int tid = threadIdx.x;
     {
@@ -121,31 +124,39 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     int bad = 0;
     for (int c0 = 0; c0 < N; c0 += DG_PW) {
         if (tid < 128) {
-            // the panel, by warps 0-3: thread t owns row j + 1 + t, kept in registers
-            // with compile-time column indices; the four warps meet at a named
-            // barrier per column (the other warps wait at the CTA barrier below)
-            for (int jj = 0; jj < DG_PW; ++jj) {
-                const int j = c0 + jj;
-                const float piv = a[j][j];
-                if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
-                const int i = j + 1 + tid;
-                if (i < N) {
-                    float prow[DG_PW], row[DG_PW];
+            // the panel, by warps 0-3: thread t keeps row c0 + t in registers for
+            // the whole panel (compile-time column indices); the owner of the
+            // pivot row publishes it to a double-buffered shared copy, and the
+            // four warps meet at a named barrier per column
+            const int i = c0 + tid;
+            float row[DG_PW];
 #pragma unroll
-                    for (int cc = 0; cc < DG_PW; ++cc) {
-                        prow[cc] = a[j][c0 + cc];
-                        row[cc] = a[i][c0 + cc];
-                    }
-                    const float l = a[i][j] / piv;
+            for (int cc = 0; cc < DG_PW; ++cc) row[cc] = i < N ? a[i][c0 + cc] : 0.f;
+            for (int jj = 0; jj < DG_PW; ++jj) {
+                float* pr = prow_buf[jj & 1];
+                if (tid == jj)
+#pragma unroll
+                    for (int cc = 0; cc < DG_PW; ++cc) pr[cc] = row[cc];
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                const float piv = pr[jj];
+                if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+                if (tid > jj && i < N) {
+                    float rj = row[0];
+#pragma unroll
+                    for (int cc = 1; cc < DG_PW; ++cc)
+                        if (cc == jj) rj = row[cc];
+                    const float l = rj / piv;
                     if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
 #pragma unroll
                     for (int cc = 0; cc < DG_PW; ++cc) {
-                        if (cc > jj) a[i][c0 + cc] = fmaf(-l, prow[cc], row[cc]);
-                        else if (cc == jj) a[i][c0 + cc] = l;
+                        if (cc > jj) row[cc] = fmaf(-l, pr[cc], row[cc]);
+                        else if (cc == jj) row[cc] = l;
                     }
                 }
-                asm volatile("bar.sync 1, 128;" ::: "memory");
             }
+            if (i < N)
+#pragma unroll
+                for (int cc = 0; cc < DG_PW; ++cc) a[i][c0 + cc] = row[cc];
         }
         __syncthreads();
         {  // U12 = L11^{-1} A12
@@ -189,23 +200,132 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
         xu[r][c] = r == c ? rd[r] : 0.f;
     }
     __syncthreads();
-    if (tid < 2 * N) {  // L^{-1}: X(r, c) = -sum_{c <= k < r} L(r, k) X(k, c)
-        const int c = tid >> 1, h = tid & 1;
-        for (int r = 1; r < N; ++r) {
+    // Inverses, blocked by 16: first the 16 x 16 diagonal blocks (a thread per
+    // block column), then one block row at a time as two small GEMMs with 4 x 4
+    // register tiles (half a shared load per FMA instead of two):
+    //   L^{-1}: X_ij = -X_ii sum_{j <= k < i} L_ik X_kj      (block rows ascending)
+    //   U^{-1}: X_ij = -X_ii sum_{i < k <= j} U_ik X_kj      (block rows descending)
+    // threads 0-255 form L^{-1}, 256-511 U^{-1}, each half with its own named barrier.
+    constexpr int B = DG_PW, NBK = N / DG_PW;
+    if (tid < N) {
+        const int blk = tid / B, c = tid % B, C = B * blk + c;
+        for (int r = c + 1; r < B; ++r) {
             float v = 0.f;
-            for (int k = c + h; k < r; k += 2) v = fmaf(a[r][k], xl[k][c], v);
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            if (h == 0 && r > c) xl[r][c] = -v;
-            __syncwarp();
+            for (int k = c; k < r; ++k) v = fmaf(a[B * blk + r][B * blk + k], xl[B * blk + k][C], v);
+            xl[B * blk + r][C] = -v;
         }
-    } else {  // U^{-1}: X(r, c) = -sum_{r < k <= c} U(r, k) X(k, c) / U(r, r)
-        const int c = (tid - 2 * N) >> 1, h = tid & 1;
-        for (int r = N - 2; r >= 0; --r) {
+    } else if (tid >= 2 * N && tid < 3 * N) {
+        const int blk = (tid - 2 * N) / B, c = (tid - 2 * N) % B, C = B * blk + c;
+        for (int r = c - 1; r >= 0; --r) {
             float v = 0.f;
-            for (int k = r + 1 + h; k <= c; k += 2) v = fmaf(a[r][k], xu[k][c], v);
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            if (h == 0 && r < c) xu[r][c] = -v * rd[r];
-            __syncwarp();
+            for (int k = r + 1; k <= c; ++k) v = fmaf(a[B * blk + r][B * blk + k], xu[B * blk + k][C], v);
+            xu[B * blk + r][C] = -v * rd[B * blk + r];
+        }
+    }
+    __syncthreads();
+    if (tid < 2 * N) {
+        const int t = tid, tr = t % 4, tc = t / 4;
+        for (int i = 1; i < NBK; ++i) {
+            const bool act = t < B * i;  // 16 i tiles of 4 x 4 over the 16 x 16 i block row
+            float acc[4][4];
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) acc[q][p] = 0.f;
+                for (int k = B * ((4 * tc) / B); k < B * i; ++k) {
+                    float av[4], xv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) av[q] = a[B * i + 4 * tr + q][k];
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xv[p] = xl[k][4 * tc + p];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(av[q], xv[p], acc[q][p]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) tl[4 * tr + q][4 * tc + p] = acc[q][p];
+            }
+            asm volatile("bar.sync 2, 256;" ::: "memory");
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) acc[q][p] = 0.f;
+#pragma unroll 4
+                for (int s2 = 0; s2 < B; ++s2) {
+                    float av[4], xv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) av[q] = xl[B * i + 4 * tr + q][B * i + s2];
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xv[p] = tl[s2][4 * tc + p];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(av[q], xv[p], acc[q][p]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xl[B * i + 4 * tr + q][4 * tc + p] = -acc[q][p];
+            }
+            asm volatile("bar.sync 2, 256;" ::: "memory");
+        }
+    } else {
+        const int t = tid - 2 * N, tr = t % 4, tc = t / 4;
+        for (int i = NBK - 2; i >= 0; --i) {
+            const int ncol = N - B * (i + 1);
+            const bool act = t < ncol;  // ncol tiles of 4 x 4 over the 16 x ncol block row
+            const int col0 = B * (i + 1) + 4 * tc;
+            float acc[4][4];
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) acc[q][p] = 0.f;
+                for (int k = B * (i + 1); k < B * (col0 / B) + B; ++k) {
+                    float av[4], xv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) av[q] = a[B * i + 4 * tr + q][k];
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xv[p] = xu[k][col0 + p];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(av[q], xv[p], acc[q][p]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) tu[4 * tr + q][col0 + p] = acc[q][p];
+            }
+            asm volatile("bar.sync 3, 256;" ::: "memory");
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) acc[q][p] = 0.f;
+#pragma unroll 4
+                for (int s2 = 0; s2 < B; ++s2) {
+                    float av[4], xv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) av[q] = xu[B * i + 4 * tr + q][B * i + s2];
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xv[p] = tu[s2][col0 + p];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(av[q], xv[p], acc[q][p]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) xu[B * i + 4 * tr + q][col0 + p] = -acc[q][p];
+            }
+            asm volatile("bar.sync 3, 256;" ::: "memory");
         }
     }
     __syncthreads();
@@ -222,7 +342,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     }
 }
 
-constexpr int DIAG_SMEM = (3 * MX_NB * DP + MX_NB) * (int)sizeof(float);
+constexpr int DIAG_SMEM = (3 * MX_NB * DP + MX_NB + 2 * DG_PW * DP) * (int)sizeof(float);
 
 void diag_group(const std::vector<DiagJob>& jobs, const MixedCtx& cx) {
     static std::once_flag attr;
