@@ -64,7 +64,7 @@ int sqbem_kernel_stats_classes(char* buf, int cap);
 
 /* Device memory: the library allocates from its own stream-ordered pool, which
  * keeps freed memory for reuse (no re-mapping between batches).  trim_pool waits
- * for the device and returns the cached memory to the driver.  (No counterpart
+ * for the device and returns the cached memory to the CUDA driver.  (No counterpart
  * in the reference, which has no device memory.) */
 int sqbem_trim_pool(void);
 

@@ -1,7 +1,7 @@
 // memory.cu -- the library's device memory pool and pinned upload staging.
 //
 // Device buffers come from one stream-ordered pool per device that keeps freed
-// memory (release threshold = max): the default pool returns it to the driver
+// memory (release threshold = max): the default pool returns it to the CUDA driver
 // at every synchronisation, and the next large allocation then has to map
 // fresh pages while the GPU waits.  sqbem_trim_pool() gives the cached memory
 // back.
