@@ -49,18 +49,56 @@ struct ConvArgs {
     ConvJob j[MAXJOBS];
 };
 
-__global__ void conv_kernel(const __grid_constant__ ConvArgs args) {
+// 32 x 32 tiles through shared memory: the loads run along the source's
+// contiguous index and the stores along the destination's, so a conversion that
+// also transposes (column-major FP32 -> row-major split) stays coalesced on
+// both sides; no 64-bit division per element.
+constexpr int CV_T = 32, CV_RY = 8;
+__global__ void __launch_bounds__(CV_T * CV_RY) conv_kernel(const __grid_constant__ ConvArgs args) {
+    __shared__ float tile[CV_T][CV_T + 1];  // [column in tile][row in tile]
     const ConvJob& J = args.j[blockIdx.y];
-    const long long total = (long long)J.rows * J.cols;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
+    const int rows = J.rows, cols = J.cols;
+    const int ntr = (rows + CV_T - 1) / CV_T, ntc = (cols + CV_T - 1) / CV_T;
+    const int t = blockIdx.x;
+    if (t >= ntr * ntc) return;
+    const int r0 = (t % ntr) * CV_T, c0 = (t / ntr) * CV_T;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const float* src = J.src;
+    const long long srs = J.s_rs, scs = J.s_cs;
+    if (srs == 1) {
+#pragma unroll
+        for (int k = 0; k < CV_T; k += CV_RY) {
+            const int r = r0 + tx, c = c0 + ty + k;
+            if (r < rows && c < cols) tile[ty + k][tx] = src[r + (long long)c * scs];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < CV_T; k += CV_RY) {
+            const int r = r0 + ty + k, c = c0 + tx;
+            if (r < rows && c < cols) tile[tx][ty + k] = src[(long long)r * srs + c * scs];
+        }
+    }
+    __syncthreads();
+    bf16* const hi = J.hi;
+    bf16* const lo = J.lo;
+    const long long drs = J.d_rs, dcs = J.d_cs;
+#pragma unroll
+    for (int k = 0; k < CV_T; k += CV_RY) {
         int r, c;
-        if (J.d_rs == 1) { r = (int)(t % J.rows); c = (int)(t / J.rows); }
-        else { c = (int)(t % J.cols); r = (int)(t / J.cols); }
-        const float x = J.src[r * J.s_rs + c * J.s_cs];
-        const bf16 h = __float2bfloat16_rn(x);
-        J.hi[r * J.d_rs + c * J.d_cs] = h;
-        J.lo[r * J.d_rs + c * J.d_cs] = __float2bfloat16_rn(x - __bfloat162float(h));
+        float x;
+        if (drs == 1) {
+            r = r0 + tx; c = c0 + ty + k;
+            x = tile[ty + k][tx];
+        } else {
+            r = r0 + ty + k; c = c0 + tx;
+            x = tile[tx][ty + k];
+        }
+        if (r < rows && c < cols) {
+            const long long o = (long long)r * drs + (long long)c * dcs;
+            const bf16 h = __float2bfloat16_rn(x);
+            hi[o] = h;
+            lo[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
     }
 }
 
@@ -547,13 +585,17 @@ void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
         ConvArgs a;
         a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
         long long mx = 0;
+        double bytes = 0;
         for (int k = 0; k < a.n; ++k) {
             a.j[k] = jobs[i0 + k];
-            mx = std::max(mx, (long long)a.j[k].rows * a.j[k].cols);
+            const long long tiles = (long long)((a.j[k].rows + CV_T - 1) / CV_T) * ((a.j[k].cols + CV_T - 1) / CV_T);
+            mx = std::max(mx, tiles);
+            bytes += 8.0 * a.j[k].rows * a.j[k].cols;  // FP32 read, two BF16 written
         }
         if (mx == 0) continue;
-        const int gx = (int)std::min<long long>(ceil_div(mx, 256), 2048);
-        TIMED_LAUNCH("convert", 0.0, 0.0, conv_kernel, dim3(gx, (unsigned)a.n), 256, 0, st, a);
+        if (mx > 0x7fffffffLL) fail(SQBEM_ERR_ARG, "convert: block too large");
+        TIMED_LAUNCH("convert", 0.0, bytes, conv_kernel, dim3((unsigned)mx, (unsigned)a.n), dim3(CV_T, CV_RY), 0, st,
+                     a);
     }
 }
 
