@@ -166,19 +166,35 @@ __global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __r
     }
 }
 
+// blockIdx.x: 256 rows, blockIdx.y: job, blockIdx.z: every gridDim.z-th column
+// (no per-element division; consecutive threads walk a column)
 __global__ void copy_kernel_g(const __grid_constant__ CopyArgs args) {
     const CopyJob& J = args.j[blockIdx.y];
-    const long long total = (long long)J.rows * J.cols;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int r = (int)(t % J.rows), c = (int)(t / J.rows);
-        const double s = J.s64 ? J.s64[r + c * J.lds] : (double)J.s32[r + c * J.lds];
-        if (J.d64) {
-            double* d = J.d64 + r + c * J.ldd;
-            *d = J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * *d);
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= J.rows) return;
+    const double* s64 = J.s64;
+    const float* s32 = J.s32;
+    double* d64 = J.d64;
+    float* d32 = J.d32;
+    const long long lds = J.lds, ldd = J.ldd;
+    const double alpha = J.alpha, beta = J.beta;
+    if (alpha == 1.0 && beta == 0.0) {  // plain copy / conversion: no FP64 arithmetic
+        for (int c = blockIdx.z; c < J.cols; c += gridDim.z) {
+            if (s32 && d32) d32[r + c * ldd] = s32[r + c * lds];
+            else if (s32) d64[r + c * ldd] = (double)s32[r + c * lds];
+            else if (d32) d32[r + c * ldd] = (float)s64[r + c * lds];
+            else d64[r + c * ldd] = s64[r + c * lds];
+        }
+        return;
+    }
+    for (int c = blockIdx.z; c < J.cols; c += gridDim.z) {
+        const double s = s64 ? s64[r + c * lds] : (double)s32[r + c * lds];
+        if (d64) {
+            double* d = d64 + r + c * ldd;
+            *d = beta == 0.0 ? alpha * s : fma(alpha, s, beta * *d);
         } else {
-            float* d = J.d32 + r + c * J.ldd;
-            *d = (float)(J.beta == 0.0 ? J.alpha * s : fma(J.alpha, s, J.beta * (double)*d));
+            float* d = d32 + r + c * ldd;
+            *d = (float)(beta == 0.0 ? alpha * s : fma(alpha, s, beta * (double)*d));
         }
     }
 }
@@ -267,13 +283,18 @@ void copy_group(const std::vector<CopyJob>& jobs_in, cudaStream_t st) {
     for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
         CopyArgs a;
         a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
-        long long mx = 0;
+        int mr = 0, mc = 0;
+        double bytes = 0;
         for (int k = 0; k < a.n; ++k) {
             a.j[k] = jobs[i0 + k];
-            mx = std::max(mx, (long long)a.j[k].rows * a.j[k].cols);
+            mr = std::max(mr, a.j[k].rows);
+            mc = std::max(mc, a.j[k].cols);
+            bytes += (double)a.j[k].rows * a.j[k].cols *
+                     ((a.j[k].s64 ? 8 : 4) + (a.j[k].d64 ? 8 : 4) * (a.j[k].beta != 0.0 ? 2 : 1));
         }
-        TIMED_LAUNCH("copy", 0.0, 0.0, copy_kernel_g,
-                     dim3((unsigned)std::min<long long>(ceil_div(mx, 256), 2048), (unsigned)a.n), 256, 0, st, a);
+        const int gz = std::min(mc, 64);
+        TIMED_LAUNCH("copy", 0.0, bytes, copy_kernel_g, dim3((unsigned)ceil_div(mr, 256), (unsigned)a.n, (unsigned)gz), 256,
+                     0, st, a);
     }
 }
 

@@ -421,8 +421,9 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     copy_group(cj, cx.st);
     cj.clear();
 
-    // r = b - A x (FP64), in three rounds that write r_t, r_s, r_c at most once each
-    auto compute_residual = [&]() {
+    // r = b - A x (FP64), in three rounds that write r_t, r_s, r_c at most once each;
+    // x_zero: x = 0 (the start of a free-swimming solve), so r = b with r_c = 0
+    auto compute_residual = [&](bool x_zero) {
         for (size_t k = 0; k < G; ++k) {
             MixedSwimmer& M = sw[k]->mx;
             if (bounded) cj.push_back(cp64(W[k].bt.get(), M.nt, W[k].rt.get(), M.nt, M.nt, r));
@@ -430,6 +431,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         }
         copy_group(cj, cx.st);
         cj.clear();
+        if (x_zero) return;
         for (int round = 0; round < 3; ++round) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
@@ -478,7 +480,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             for (int c = 0; c < r; ++c) out[k * r + c] = h[4 * r * k + c] + h[4 * r * k + r + c] + h[4 * r * k + 2 * r + c];
         return out;
     };
-    compute_residual();
+    compute_residual(!prescribed);  // r_c was zeroed with x above
     const std::vector<double> r0 = norms();
     int it = 0;
     double worst = 0;
@@ -567,7 +569,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         copy_group(cj, cx.st);
         cj.clear();
         // (h) new residual
-        compute_residual();
+        compute_residual(false);
         const std::vector<double> rn = norms();
         worst = 0;
         for (size_t k = 0; k < G * r; ++k) {
