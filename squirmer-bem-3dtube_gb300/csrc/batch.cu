@@ -63,6 +63,33 @@ Prepared prepare(const sqbem_instance& in) {
     return p;
 }
 
+// prepare() of every instance, spread over up to 8 host threads (mesh
+// generation is host work on the end-to-end path).
+std::vector<Prepared> prepare_all(int n, const sqbem_instance* inst) {
+    std::vector<Prepared> prep((size_t)n);
+    const int W = std::max(1, std::min(8, n / 4));
+    std::atomic<int> next{0};
+    std::exception_ptr err;
+    std::mutex emu;
+    auto work = [&]() {
+        try {
+            for (int k; (k = next.fetch_add(1)) < n;) prep[k] = prepare(inst[k]);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(emu);
+            if (!err) err = std::current_exception();
+        }
+    };
+    if (W == 1) {
+        work();
+    } else {
+        std::vector<std::thread> th;
+        for (int w = 0; w < W; ++w) th.emplace_back(work);
+        for (auto& t : th) t.join();
+    }
+    if (err) std::rethrow_exception(err);
+    return prep;
+}
+
 void validate(const sqbem_instance& in) {
     if (!(in.a_over_R >= 0 && in.a_over_R < 1) || !(in.beta >= 0 && in.beta < 1) || !(in.L_over_R > 0) ||
         in.sphere_level < 0 || in.sphere_level > 5 || (in.a_over_R > 0 && (in.n_theta < 3 || in.n_r < 1)))
@@ -164,7 +191,7 @@ void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_ins
         }
     }
     pc.lap("setup", G, ntp_k, ns_k);
-    if (!tp.empty()) mixed_build_tubes(tp, cx);
+    if (!tp.empty()) mixed_build_tubes(tp, cx, /*explicit_inverse=*/false);  // each tube serves one swimmer
     pc.lap("tubes", G, ntp_k, ns_k);
     for (size_t g = 0; g < G; ++g) {
         const Prepared& P = prep[ids[g]];
@@ -322,9 +349,7 @@ extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int pre
         if (device_seconds) *device_seconds = 0;
         if (n == 0) return;
         require_device();
-        std::vector<Prepared> prep;
-        prep.reserve(n);
-        for (int k = 0; k < n; ++k) prep.push_back(prepare(inst[k]));
+        const std::vector<Prepared> prep = prepare_all(n, inst);
         Stream bs;
         EventTimer clk;
         clk.start(bs);
@@ -350,9 +375,7 @@ extern "C" int sqbem_adjoint_batch(int n, const sqbem_instance* inst, int precis
         Stream bs;
         EventTimer clk;
         clk.start(bs);
-        std::vector<Prepared> prep;
-        prep.reserve(n);
-        for (int k = 0; k < n; ++k) prep.push_back(prepare(inst[k]));
+        const std::vector<Prepared> prep = prepare_all(n, inst);
         std::vector<double> bytes;
         for (int k = 0; k < n; ++k) {
             const double t = 3.0 * (prep[k].bounded ? prep[k].tube.P() : 0), sp = 3.0 * prep[k].sphere.P();

@@ -599,6 +599,125 @@ void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
     }
 }
 
+// ---------------------------------------------------------------- triangular solves, few right-hand sides
+// x <- U^{-1} L^{-1} x for R <= 2 columns, one CTA per member.  The solve runs
+// by 128-row blocks: s = x_i - (off-diagonal blocks) x, by a warp per row
+// reading the row-major split factor along its contiguous index (hi + lo,
+// coalesced) against x held in shared memory; then x_i = inv(diag block) s
+// with the FP32 block inverses.  Input and output are FP64 (rows beyond n_true
+// are zero); the arithmetic is FP32 like the tensor-core solves.
+constexpr int TS_THREADS = 1024;
+struct TrsvJob {
+    const bf16* Rh;
+    const bf16* Rl;
+    const float* Li;
+    const float* Ui;
+    const double* in;
+    long long ldi;
+    double* out;
+    long long ldo;
+    int n_true;
+};
+struct TrsvArgs {
+    int n, r;
+    TrsvJob j[MAXJOBS];
+};
+
+template <int R>
+__global__ void __launch_bounds__(TS_THREADS) trsv_kernel(const __grid_constant__ TrsvArgs args) {
+    extern __shared__ float tsm[];
+    const TrsvJob& J = args.j[blockIdx.x];
+    const int n = args.n, nt = J.n_true, r = args.r;
+    float* x = tsm;                   // n x R, x[row * R + c]
+    float* sb = tsm + (size_t)n * R;  // 128 x R block of sums
+    const bf16* Rh = J.Rh;
+    const bf16* Rl = J.Rl;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int e = tid; e < n * R; e += TS_THREADS) {
+        const int row = e / R, c = e % R;
+        x[e] = (row < nt && c < r) ? (float)J.in[row + c * J.ldi] : 0.f;
+    }
+    __syncthreads();
+    const int nb = n / MX_NB;
+    for (int pass = 0; pass < 2; ++pass) {  // 0: L (forward), 1: U (backward)
+        for (int step = 0; step < nb; ++step) {
+            const int b = pass == 0 ? step : nb - 1 - step;
+            const int k0 = pass == 0 ? 0 : (b + 1) * MX_NB, k1 = pass == 0 ? b * MX_NB : n;
+            // s = x_b - A(b rows, [k0, k1)) x([k0, k1)): 4 rows per warp, each lane
+            // loading 8 consecutive entries (16 bytes) of hi and of lo per step
+            for (int rl = warp; rl < MX_NB; rl += TS_THREADS / 32) {
+                const int row = b * MX_NB + rl;
+                float acc[R];
+#pragma unroll
+                for (int c = 0; c < R; ++c) acc[c] = 0.f;
+                const long long base = (long long)row * n;
+#pragma unroll 2
+                for (int k = k0 + 8 * lane; k < k1; k += 256) {
+                    const uint4 hv = *reinterpret_cast<const uint4*>(Rh + base + k);
+                    const uint4 lv = *reinterpret_cast<const uint4*>(Rl + base + k);
+                    const bf16* hp = reinterpret_cast<const bf16*>(&hv);
+                    const bf16* lp = reinterpret_cast<const bf16*>(&lv);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float a = __bfloat162float(hp[q]) + __bfloat162float(lp[q]);
+#pragma unroll
+                        for (int c = 0; c < R; ++c) acc[c] = fmaf(a, x[(k + q) * R + c], acc[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < R; ++c) {
+                    float v = acc[c];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) sb[rl * R + c] = x[row * R + c] - v;
+                }
+            }
+            __syncthreads();
+            // x_b = inv(diag block b) s   (column-major 128 x 128 FP32 inverse)
+            const float* Inv = (pass == 0 ? J.Li : J.Ui) + (size_t)b * MX_NB * MX_NB;
+            for (int e = tid; e < MX_NB * R; e += TS_THREADS) {
+                const int rl = e % MX_NB, c = e / MX_NB;
+                float v = 0.f;
+                for (int q = 0; q < MX_NB; ++q) v = fmaf(Inv[rl + q * MX_NB], sb[q * R + c], v);
+                x[(b * MX_NB + rl) * R + c] = v;
+            }
+            __syncthreads();
+        }
+    }
+    for (int e = tid; e < nt * R; e += TS_THREADS) {
+        const int row = e / R, c = e % R;
+        if (c < r) J.out[row + c * J.ldo] = (double)x[e];
+    }
+}
+
+void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
+                const std::vector<double*>& out, const std::vector<int>& n_true, int r, cudaStream_t st) {
+    if (g.empty()) return;
+    if (r < 1 || r > 2) fail(SQBEM_ERR_ARG, "trsv: 1 or 2 right-hand sides");
+    const int n = g[0]->n;
+    const size_t smem = ((size_t)n + MX_NB) * 2 * sizeof(float);
+    if (smem > 227 * 1024) fail(SQBEM_ERR_ARG, "trsv: %d unknowns exceed shared memory", n);
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        CUDA_CHECK(cudaFuncSetAttribute(trsv_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    });
+    for (size_t i0 = 0; i0 < g.size(); i0 += MAXJOBS) {
+        TrsvArgs a;
+        a.n = n;
+        a.r = r;
+        const int m = (int)std::min<size_t>(MAXJOBS, g.size() - i0);
+        for (int k = 0; k < m; ++k) {
+            const MixedLU& L = *g[i0 + k];
+            if (L.n != n) fail(SQBEM_ERR_ARG, "trsv: group members differ in size");
+            const int nt = n_true[i0 + k];
+            if (nt < 1 || nt > n) fail(SQBEM_ERR_ARG, "trsv: bad row count");
+            a.j[k] = {L.Rh.get(), L.Rl.get(), L.Li.get(), L.Ui.get(), in[i0 + k], nt, out[i0 + k], nt, nt};
+        }
+        const double by = (double)m * ((double)n * n * 4.0 + 2.0 * n * r * 8.0);
+        TIMED_LAUNCH("trsv", 0.0, by, trsv_kernel<2>, m, TS_THREADS, smem, st, a);
+    }
+}
+
 void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx) {
     if (g.empty()) return;
     const int n = g[0]->n;

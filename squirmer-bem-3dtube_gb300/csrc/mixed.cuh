@@ -70,4 +70,11 @@ struct ConvJob {
 };
 void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st);
 
+// out <- A^{-1} in for every member's factor (n_true[k] x r, r <= 2, FP64 in and
+// out, leading dimension n_true[k]), one CTA per member: the block forward and
+// backward substitutions with the split factor and the block inverses, for
+// refinement corrections.
+void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
+                const std::vector<double*>& out, const std::vector<int>& n_true, int r, cudaStream_t st);
+
 }  // namespace sqbem

@@ -163,7 +163,7 @@ static void invert_group(const std::vector<MixedLU*>& L, const std::vector<float
 }
 
 // ---------------------------------------------------------------- tubes
-void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx) {
+void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx, bool explicit_inverse) {
     const size_t G = tubes.size();
     std::vector<MixedLU> lu(G);
     std::vector<MixedLU*> lus;
@@ -187,6 +187,15 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
     copy_group(cj, cx.st);
     mixed_lu_factor(lus, cx);
     check_ctx(cx, "dgetrf (mixed tube factor)");
+    if (!explicit_inverse) {
+        for (size_t k = 0; k < G; ++k) {
+            lu[k].A.release();  // the solves read only the split factor and the block inverses
+            lu[k].Ch.release();
+            lu[k].Cl.release();
+            tubes[k]->mt.lu = std::make_unique<MixedLU>(std::move(lu[k]));
+        }
+        return;
+    }
     std::vector<float*> inv;
     std::vector<bf16*> rh, rl;
     for (sqbem_tube* t : tubes) {
@@ -288,20 +297,54 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             MixedSwimmer& M = sw[k]->mx;
             const int ntp = sw[k]->tube->mt.ntp;
             const size_t sz = (size_t)ntp * M.nc;
-            bch[k].alloc(sz, cx.st); bcl[k].alloc(sz, cx.st); bch[k].zero(); bcl[k].zero();
+            if (sw[k]->tube->mt.explicit_inverse()) {
+                bch[k].alloc(sz, cx.st); bcl[k].alloc(sz, cx.st); bch[k].zero(); bcl[k].zero();
+            }
             yh[k].alloc(sz, cx.st); yl[k].alloc(sz, cx.st); yh[k].zero(); yl[k].zero();
             dh[k].alloc((size_t)M.ns * ntp, cx.st); dl[k].alloc((size_t)M.ns * ntp, cx.st);
             dh[k].zero(); dl[k].zero();
-            conv.push_back({M.B.get(), 1, M.nt, M.nt, M.ns, bch[k].get(), bcl[k].get(), 1, ntp});
-            conv.push_back({M.Ct.get(), 1, M.nt, M.nt, 6, bch[k].get() + (size_t)ntp * M.ns,
-                            bcl[k].get() + (size_t)ntp * M.ns, 1, ntp});
+            if (sw[k]->tube->mt.explicit_inverse()) {  // the operand of Y = T^{-1} [B | Ct]
+                conv.push_back({M.B.get(), 1, M.nt, M.nt, M.ns, bch[k].get(), bcl[k].get(), 1, ntp});
+                conv.push_back({M.Ct.get(), 1, M.nt, M.nt, 6, bch[k].get() + (size_t)ntp * M.ns,
+                                bcl[k].get() + (size_t)ntp * M.ns, 1, ntp});
+            }
             conv.push_back({M.D.get(), 1, M.ns, M.ns, M.nt, dh[k].get(), dl[k].get(), ntp, 1});
         }
         convert_group(conv, cx.st);
         // Y = T^{-1} [B | Ct]   (FP32 for the refinement, split for the Schur product)
         std::vector<TcProblem> P;
         std::vector<TcOperands> O;
-        for (size_t k = 0; k < G; ++k) {
+        if (!sw[0]->tube->mt.explicit_inverse()) {
+            // by the LU solves: X = [B | Ct] padded to ntp rows, solved in place; the
+            // solves keep the column-major split copy (yh, yl) equal to the result
+            std::vector<DevBuf<float>> yp(G);
+            std::vector<MixedLU*> tl;
+            std::vector<Rhs> rhs(G);
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const MixedTube& Tt = sw[k]->tube->mt;
+                if (Tt.explicit_inverse()) fail(SQBEM_ERR_ARG, "mixed swimmers of one group share a tube mode");
+                const int ntp = Tt.ntp;
+                yp[k].alloc((size_t)ntp * M.nc, cx.st);
+                yp[k].zero();
+                cj.push_back(cp32_32(M.B.get(), M.nt, yp[k].get(), ntp, M.nt, M.ns));
+                cj.push_back(cp32_32(M.Ct.get(), M.nt, yp[k].get() + (size_t)ntp * M.ns, ntp, M.nt, 6));
+                tl.push_back(Tt.lu.get());
+                Rhs& r = rhs[k];
+                r.X = yp[k].get(); r.ldx = ntp; r.nrhs = M.nc; r.Sh = yh[k].get(); r.Sl = yl[k].get(); r.lds = ntp;
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+            mixed_lu_solve(tl, rhs, cx);
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                M.Y.alloc((size_t)M.nt * M.nc, cx.st);
+                cj.push_back(cp32_32(yp[k].get(), sw[k]->tube->mt.ntp, M.Y.get(), M.nt, M.nt, M.nc));
+            }
+            copy_group(cj, cx.st);
+            cj.clear();
+        }
+        for (size_t k = 0; k < G && sw[0]->tube->mt.explicit_inverse(); ++k) {
             MixedSwimmer& M = sw[k]->mx;
             const MixedTube& Tt = sw[k]->tube->mt;
             const int ntp = Tt.ntp;
@@ -316,7 +359,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             P.push_back(p);
             O.push_back(o);
         }
-        tc_gemm(P, O, cx.err, nullptr, cx.st);
+        if (!P.empty()) tc_gemm(P, O, cx.err, nullptr, cx.st);
         P.clear();
         O.clear();
         // [G_s | G_c] -= D Y
@@ -391,6 +434,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     struct Work {
         DevBuf<double> bt, bs, rt, rs, rc, rsp, yt, tmp6, dsw, dt, nrm;
     };
+    const bool factor_mode = bounded && !sw[0]->tube->mt.explicit_inverse();
     std::vector<Work> W(G);
     std::vector<MvJob> mj;
     std::vector<CopyJob> cj;
@@ -490,7 +534,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         for (size_t k = 0; k < G; ++k) {
             MixedSwimmer& M = sw[k]->mx;
             cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
-            if (bounded) {
+            if (bounded && !factor_mode) {
                 const MixedTube& Tt = sw[k]->tube->mt;
                 mj.push_back(mv32(Tt.Ti.get(), Tt.ntp, M.nt, M.nt, W[k].rt.get(), M.nt, r, W[k].yt.get(), M.nt, 1.0, 0.0));
             }
@@ -499,6 +543,19 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         cj.clear();
         matvec_group(mj, cx.st);
         mj.clear();
+        if (factor_mode) {  // y_t by the block substitutions of the tube factor (one launch)
+            std::vector<const MixedLU*> tl;
+            std::vector<const double*> ins;
+            std::vector<double*> outs;
+            std::vector<int> nts;
+            for (size_t k = 0; k < G; ++k) {
+                tl.push_back(sw[k]->tube->mt.lu.get());
+                ins.push_back(W[k].rt.get());
+                outs.push_back(W[k].yt.get());
+                nts.push_back(sw[k]->mx.nt);
+            }
+            trsv_group(tl, ins, outs, nts, r, cx.st);
+        }
         if (bounded) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;

@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include <memory>
 #include <vector>
 
 #include "common.cuh"
@@ -28,8 +29,14 @@ constexpr int REFINE_MAX_IT = 30;
 struct MixedTube {
     int nt = 0, ntp = 0;          // 3 Nt and its multiple of 128
     DevBuf<float> T;              // deflated T (nt x nt, column-major, ld nt), FP32
+    // explicit inverse (a tube shared by many swimmers: trajectories, the
+    // single-swimmer API) ...
     DevBuf<float> Ti;             // T^{-1}, ntp x ntp column-major (padding: identity)
     DevBuf<bf16> TiRh, TiRl;      // T^{-1} split row-major (left operand of Y = T^{-1}[B | Ct])
+    // ... or, for a tube used by one swimmer (the batches), its factor only: Y and
+    // the refinement's T^{-1} r come from LU solves, which saves forming T^{-1}
+    std::unique_ptr<MixedLU> lu;  // split factor and diagonal-block inverses (A, Ch, Cl released)
+    bool explicit_inverse() const { return !lu; }
 };
 
 struct MixedSwimmer {
@@ -57,7 +64,7 @@ struct MixedCtx;
 // Build the mixed tubes / swimmers of a group (equal padded tube size; for the
 // swimmers also equal sphere size).  The assembly runs per member, the dense
 // steps as grouped launches.
-void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx);
+void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx, bool explicit_inverse = true);
 void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx);
 // Refined solve of every member for nrhs right-hand sides; x = [f_t; f_s; w]
 // per member (device, FP64, (nt + nc) x nrhs), plus the iterations used and the
