@@ -25,9 +25,9 @@
 //                swimmer.hpp:218-220), computed by a fixed-order reduction over
 //                the stored D block (deterministic).
 // Precision: FP64 everywhere in SQBEM_FP64 mode.  In SQBEM_MIXED mode the
-// relative vectors e_k = V_k - x0 and the rule choice are FP64, the far (7) and
-// near (28/112) rules are evaluated in FP32 from those accurate vectors, and the
-// 448-point near-singular rule and the Duffy self integrals stay FP64.
+// relative vectors (vertex and centroid offsets) and the rule choice are FP64,
+// rounded once; every rule (7 to 448 points) and the Duffy self integrals are
+// then evaluated in FP32 (GB300's FP64 pipe runs at about 1/64 of the FP32 rate).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -54,6 +54,7 @@ __constant__ QPoint c_rule7[7];
 __constant__ QPointF c_rule7f[7];
 __device__ double d_gl_x[10], d_gl_w[10];
 __device__ QPoint d_duffy[100];  // (x_a, x_b, w_a * w_b) for the 10 x 10 GL grid
+__device__ QPointF d_duffyf[100];
 
 static std::once_flag g_table_once[64];
 
@@ -82,6 +83,9 @@ void init_tables() {
         for (int a = 0; a < 10; ++a)
             for (int b = 0; b < 10; ++b) duf.push_back({gx[a], gx[b], 0.0, gw[a] * gw[b]});
         CUDA_CHECK(cudaMemcpyToSymbol(d_duffy, duf.data(), sizeof(QPoint) * 100));
+        std::vector<QPointF> duff;
+        for (const QPoint& q : duf) duff.push_back({(float)q.l0, (float)q.l1, 0.f, (float)q.w});
+        CUDA_CHECK(cudaMemcpyToSymbol(d_duffyf, duff.data(), sizeof(QPointF) * 100));
         CUDA_CHECK(cudaDeviceSynchronize());
     });
 }
@@ -248,6 +252,36 @@ __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y,
     warp_reduce(A);
 }
 
+// FP32 Duffy self integral for the mixed path: the vertex offsets V_k - x0 are
+// formed in FP64 by lanes 0..8, rounded once and broadcast; the sub-triangle
+// Jacobians and the 300 points are FP32 (r = u[(1 - v) e1 + v e2] has no
+// cancellation, and u / |r| is bounded).
+__device__ void warp_self_f32(Acc<float>& A, const PanelRec* Pg, double x, double y, double z, int lane) {
+    A.zero();
+    float val = 0.f;
+    if (lane < 9) val = (float)(Pg->v[lane] - (lane % 3 == 0 ? x : lane % 3 == 1 ? y : z));
+    float d[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[k] = __shfl_sync(0xffffffffu, val, k);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int f = e == 2 ? 0 : e + 1;
+        const float e1x = d[3 * e], e1y = d[3 * e + 1], e1z = d[3 * e + 2];
+        const float e2x = d[3 * f], e2y = d[3 * f + 1], e2z = d[3 * f + 2];
+        const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+        const float J = sqrtf(cx * cx + cy * cy + cz * cz);
+        for (int g = lane; g < 100; g += 32) {
+            const QPointF Q = d_duffyf[g];
+            const float u = Q.l0, v = Q.l1;
+            const float rx = u * ((1.f - v) * e1x + v * e2x);
+            const float ry = u * ((1.f - v) * e1y + v * e2y);
+            const float rz = u * ((1.f - v) * e1z + v * e2z);
+            accum<float, false>(A, rx, ry, rz, Q.w * u * J, 0.f, 0.f, 0.f);
+        }
+    }
+    warp_reduce(A);
+}
+
 // ---------------------------------------------------------------- far kernel
 constexpr int FAR_TGT = 64;   // targets per CTA (threads)
 constexpr int FAR_SRC = 16;   // source panels per CTA
@@ -367,11 +401,15 @@ __global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
         const int rule = e.y >> 28;  // exact rule (4 = self), decided by the far kernel
         double sl = 0, dl = 0;
         const int a = lane / 3, b = lane % 3;
-        if (rule == 4) {
+        if (MIXED && rule == 4) {
+            Acc<float> A;
+            warp_self_f32(A, job.src + p, x, y, z, lane);
+            if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
+        } else if (rule == 4) {
             Acc<double> A;
             warp_self(A, P, x, y, z, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
-        } else if (MIXED && rule < 3) {
+        } else if (MIXED) {
             Acc<float> A;
             warp_rule_f32(A, job.src + p, x, y, z, rule, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
