@@ -287,15 +287,26 @@ constexpr int FAR_TGT = 64;   // targets per CTA (threads)
 constexpr int FAR_SRC = 16;   // source panels per CTA
 
 // FP32 view of a source panel for the mixed far field: vertex offsets from the
-// centroid (exact in FP64, rounded once), normal, area, and the FP64 squared
-// far-field radius (3 h)^2 of the rule test.
+// centroid (exact in FP64, rounded once), normal, area, the centroid as an
+// unevaluated sum hi + lo of two floats, and the squared far-field radius
+// (3 h)^2: in FP64 for the exact test and, raised by 1e-5, in FP32 for the
+// quick one.
 struct FarF {
     float d[9];
     float n[3];
     float area;
-    float pad;
+    float far2f;
+    float chi[3], clo[3];
     double far2;
 };
+
+// v = hi + lo with hi = fl32(v) and lo = fl32(v - hi): the pair carries v to
+// about 2^-48 relative, so a difference of two such pairs formed in FP32,
+// (a_hi - b_hi) + (a_lo - b_lo), is within ~2.5 FP32 ulps of the exact one.
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
 
 template <class TO, class TC>
 __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
@@ -318,12 +329,20 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
             F.n[0] = (float)P.n[0]; F.n[1] = (float)P.n[1]; F.n[2] = (float)P.n[2];
             F.area = (float)P.area;
             F.far2 = 9.0 * P.h * P.h;
+            F.far2f = (float)(F.far2 * (1.0 + 1e-5));
+            for (int k = 0; k < 3; ++k) split2(P.c[k], F.chi[k], F.clo[k]);
         }
         __syncthreads();
     }
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     if (i >= job.nT) return;
     const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
+    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+    if constexpr (sizeof(TC) == 4) {
+        split2(x, xh, xl);
+        split2(y, yh, yl);
+        split2(z, zh, zl);
+    }
     const TC ss = (TC)job.sscale, ds = (TC)job.dscale;
     for (int s = 0; s < ns; ++s) {
         const PanelRec& P = sp[s];
@@ -349,23 +368,31 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
                                     l0 * e0z + l1 * e1z + l2 * e2z, w * area, mx, my, mz);
             }
         } else {
-            // rule test on the squared distance in FP64; the reference's exact test
-            // (sqrt, division) only inside a +-1e-12 band around the threshold
-            const double cx = P.c[0] - x, cy = P.c[1] - y, cz = P.c[2] - z;
-            const double d2 = cx * cx + cy * cy + cz * cz;
+            // c - x0 from the hi + lo pairs (relative error <= ~2.5 ulp per
+            // component, so d2 is within ~5e-7 of the exact value).  A pair is far
+            // without further test when d2 clears (3 h)^2 by 1e-5; otherwise the
+            // FP64 test on the squared distance decides, and the reference's exact
+            // test (sqrt, division) runs inside a +-1e-12 band around the threshold
+            // and for every near pair -- the same rule as a pure FP64 decision.
             const FarF& F = sf[s];
-            // exact rule only for pairs that are near or inside the band (the near
-            // kernel takes the rule from the list)
+            const float bx = (F.chi[0] - xh) + (F.clo[0] - xl);
+            const float by = (F.chi[1] - yh) + (F.clo[1] - yl);
+            const float bz = (F.chi[2] - zh) + (F.clo[2] - zl);
             int rule = 0;
-            if (self) rule = 4;
-            else if (!(d2 > F.far2 * (1.0 + 1e-12))) rule = rule_of(P, x, y, z);
+            if (self) {
+                rule = 4;
+            } else if (!(bx * bx + by * by + bz * bz > F.far2f)) {
+                const double cx = P.c[0] - x, cy = P.c[1] - y, cz = P.c[2] - z;
+                const double d2 = cx * cx + cy * cy + cz * cz;
+                // the near kernel takes the exact rule from the list
+                if (!(d2 > F.far2 * (1.0 + 1e-12))) rule = rule_of(P, x, y, z);
+            }
             if (rule != 0) {
                 const int slot = atomicAdd(job.near_count, 1);
                 if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
                 continue;
             }
-            // r = (c - x0) + sum_k l_k (V_k - c): FP64 only in the centroid offset
-            const float bx = (float)cx, by = (float)cy, bz = (float)cz;
+            // r = (c - x0) + sum_k l_k (V_k - c)
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
                 const float l0 = c_rule7f[q].l0, l1 = c_rule7f[q].l1, l2 = c_rule7f[q].l2, w = c_rule7f[q].w;
