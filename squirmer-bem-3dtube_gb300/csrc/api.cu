@@ -237,6 +237,22 @@ extern "C" int sqbem_panel_integrals(int n, const double* V9, const double* x0, 
     });
 }
 
+// Test hook, not part of the public ABI: the mixed path's FP64 reciprocal
+// square root on n host values (its error bound is checked by the GPU tests).
+extern "C" int sqbem_test_rsqrt_nr(int n, const double* x, double* y) {
+    return guarded([&] {
+        if (n < 0 || (n > 0 && (!x || !y))) fail(SQBEM_ERR_ARG, "test_rsqrt_nr: bad arguments");
+        if (n == 0) return;
+        require_device();
+        Stream s;
+        DevBuf<double> dx(n, s), dy(n, s);
+        dx.upload(x, n);
+        rsqrt_nr_eval(n, dx.get(), dy.get(), s);
+        dy.download(y, n);
+        CUDA_CHECK(cudaStreamSynchronize(s));
+    });
+}
+
 // ---------------------------------------------------------------- dense
 extern "C" int sqbem_solve_dense(int n, int nrhs, const double* A, double* B, int* pivoted) {
     return guarded([&] {

@@ -26,8 +26,9 @@
 //                the stored D block (deterministic).
 // Precision: FP64 everywhere in SQBEM_FP64 mode.  In SQBEM_MIXED mode the
 // relative vectors (vertex and centroid offsets) and the rule choice are FP64,
-// rounded once; every rule (7 to 448 points) and the Duffy self integrals are
-// then evaluated in FP32 (GB300's FP64 pipe runs at about 1/64 of the FP32 rate).
+// rounded once; the far (7) and near (28/112) rules are evaluated in FP32 from
+// them, while the 448-point near-singular rule and the Duffy self integrals stay
+// FP64, with a reciprocal square root refined from an FP32 seed (rsqrt_nr).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -54,7 +55,6 @@ __constant__ QPoint c_rule7[7];
 __constant__ QPointF c_rule7f[7];
 __device__ double d_gl_x[10], d_gl_w[10];
 __device__ QPoint d_duffy[100];  // (x_a, x_b, w_a * w_b) for the 10 x 10 GL grid
-__device__ QPointF d_duffyf[100];
 
 static std::once_flag g_table_once[64];
 
@@ -83,9 +83,6 @@ void init_tables() {
         for (int a = 0; a < 10; ++a)
             for (int b = 0; b < 10; ++b) duf.push_back({gx[a], gx[b], 0.0, gw[a] * gw[b]});
         CUDA_CHECK(cudaMemcpyToSymbol(d_duffy, duf.data(), sizeof(QPoint) * 100));
-        std::vector<QPointF> duff;
-        for (const QPoint& q : duf) duff.push_back({(float)q.l0, (float)q.l1, 0.f, (float)q.w});
-        CUDA_CHECK(cudaMemcpyToSymbol(d_duffyf, duff.data(), sizeof(QPointF) * 100));
         CUDA_CHECK(cudaDeviceSynchronize());
     });
 }
@@ -98,14 +95,32 @@ struct Acc {
     __device__ void zero() { dg = sxx = sxy = sxz = syy = syz = szz = dxx = dxy = dxz = dyy = dyz = dzz = T(0); }
 };
 
-__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+// 1/sqrt(x) in FP64 for the mixed path's near-singular and self integrals: the
+// FP32 seed y0 = rsqrtf(x) (relative error e0 below ~2^-21.5, including the
+// rounding of x to FP32) refined by one Newton step for f(y) = 1/y^2 - x,
+// y1 = y0 (3 - x y0^2) / 2, whose relative error is 1.5 e0^2 + O(e0^3) < 1e-13.
+// Four FP64 operations instead of a full-precision FP64 reciprocal square root.
+// x is a squared distance between quadrature point and target, far inside the
+// FP32 range (and never 0: the Duffy and Gauss points are interior).
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    const double y = (double)rsqrtf((float)x);
+    return y * fma(-0.5 * x * y, y, 1.5);
+}
+
+template <bool NR>
+__device__ __forceinline__ double rsqrt_t(double x) {
+    if constexpr (NR) return rsqrt_nr(x);
+    else return rsqrt(x);
+}
+template <bool NR>
 __device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 
 // One quadrature node: accumulate w G(r) and w T(r).m (kernels.hpp:29-40).
-template <class T, bool WITH_DL>
+// NR: FP64 with rsqrt_nr (the mixed path's FP64 integrals).
+template <class T, bool WITH_DL, bool NR = false>
 __device__ __forceinline__ void accum(Acc<T>& A, T rx, T ry, T rz, T w, T mx, T my, T mz) {
     const T r2 = rx * rx + ry * ry + rz * rz;
-    const T ir = rsqrt_t(r2);
+    const T ir = rsqrt_t<NR>(r2);
     const T ir2 = ir * ir;
     const T ir3 = ir * ir2;
     const T s = w * ir3;
@@ -171,7 +186,7 @@ __device__ __forceinline__ int rule_of(const PanelRec& P, double x, double y, do
 // Sum over one rule's points split across the 32 lanes of a warp (after the
 // call every lane holds the complete sums).  FP64 or FP32 evaluation from the
 // FP64 relative vertex vectors e_k = V_k - x0.
-template <class T>
+template <class T, bool NR = false>
 __device__ void warp_rule(Acc<T>& A, const PanelRec& P, double x, double y, double z, int rule, int lane) {
     A.zero();
     const T e0x = (T)(P.v[0] - x), e0y = (T)(P.v[1] - y), e0z = (T)(P.v[2] - z);
@@ -192,7 +207,7 @@ __device__ void warp_rule(Acc<T>& A, const PanelRec& P, double x, double y, doub
         const T rx = l0 * e0x + l1 * e1x + l2 * e2x;
         const T ry = l0 * e0y + l1 * e1y + l2 * e2y;
         const T rz = l0 * e0z + l1 * e1z + l2 * e2z;
-        accum<T, true>(A, rx, ry, rz, w * area, mx, my, mz);
+        accum<T, true, NR>(A, rx, ry, rz, w * area, mx, my, mz);
     }
     warp_reduce(A);
 }
@@ -231,6 +246,7 @@ __device__ void warp_rule_f32(Acc<float>& A, const PanelRec* Pg, double x, doubl
 // sub-triangles (x0, V_e, V_e+1), x = x0 + u[(1 - v) e1 + v e2], Jacobian u J.
 // The edge vectors and J are formed once per sub-triangle; the lanes split its
 // 10 x 10 points.
+template <bool NR = false>
 __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y, double z, int lane) {
     A.zero();
 #pragma unroll
@@ -246,37 +262,7 @@ __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y,
             const double rx = u * ((1 - v) * e1x + v * e2x);
             const double ry = u * ((1 - v) * e1y + v * e2y);
             const double rz = u * ((1 - v) * e1z + v * e2z);
-            accum<double, false>(A, rx, ry, rz, Q.w * u * J, 0.0, 0.0, 0.0);
-        }
-    }
-    warp_reduce(A);
-}
-
-// FP32 Duffy self integral for the mixed path: the vertex offsets V_k - x0 are
-// formed in FP64 by lanes 0..8, rounded once and broadcast; the sub-triangle
-// Jacobians and the 300 points are FP32 (r = u[(1 - v) e1 + v e2] has no
-// cancellation, and u / |r| is bounded).
-__device__ void warp_self_f32(Acc<float>& A, const PanelRec* Pg, double x, double y, double z, int lane) {
-    A.zero();
-    float val = 0.f;
-    if (lane < 9) val = (float)(Pg->v[lane] - (lane % 3 == 0 ? x : lane % 3 == 1 ? y : z));
-    float d[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) d[k] = __shfl_sync(0xffffffffu, val, k);
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-        const int f = e == 2 ? 0 : e + 1;
-        const float e1x = d[3 * e], e1y = d[3 * e + 1], e1z = d[3 * e + 2];
-        const float e2x = d[3 * f], e2y = d[3 * f + 1], e2z = d[3 * f + 2];
-        const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
-        const float J = sqrtf(cx * cx + cy * cy + cz * cz);
-        for (int g = lane; g < 100; g += 32) {
-            const QPointF Q = d_duffyf[g];
-            const float u = Q.l0, v = Q.l1;
-            const float rx = u * ((1.f - v) * e1x + v * e2x);
-            const float ry = u * ((1.f - v) * e1y + v * e2y);
-            const float rz = u * ((1.f - v) * e1z + v * e2z);
-            accum<float, false>(A, rx, ry, rz, Q.w * u * J, 0.f, 0.f, 0.f);
+            accum<double, false, NR>(A, rx, ry, rz, Q.w * u * J, 0.0, 0.0, 0.0);
         }
     }
     warp_reduce(A);
@@ -428,21 +414,17 @@ __global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
         const int rule = e.y >> 28;  // exact rule (4 = self), decided by the far kernel
         double sl = 0, dl = 0;
         const int a = lane / 3, b = lane % 3;
-        if (MIXED && rule == 4) {
-            Acc<float> A;
-            warp_self_f32(A, job.src + p, x, y, z, lane);
-            if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
-        } else if (rule == 4) {
+        if (rule == 4) {
             Acc<double> A;
-            warp_self(A, P, x, y, z, lane);
+            warp_self<MIXED>(A, P, x, y, z, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = 0.0; }
-        } else if (MIXED) {
+        } else if (MIXED && rule < 3) {
             Acc<float> A;
             warp_rule_f32(A, job.src + p, x, y, z, rule, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
         } else {
             Acc<double> A;
-            warp_rule<double>(A, P, x, y, z, rule, lane);
+            warp_rule<double, MIXED>(A, P, x, y, z, rule, lane);
             if (lane < 9) { sl = sl_entry(A, a, b); dl = dl_entry(A, a, b); }
         }
         if (lane < 9) {
@@ -671,7 +653,8 @@ __global__ void __launch_bounds__(FIELD_WARPS * 32) field_kernel(FieldJob job) {
             for (int q = 0; q < 9; ++q) { sl[q] = sl_entry(A, q / 3, q % 3); dl[q] = dl_entry(A, q / 3, q % 3); }
         } else {
             Acc<double> A;
-            warp_rule<double>(A, P, x, y, z, rule, lane);
+            if (job.mixed) warp_rule<double, true>(A, P, x, y, z, rule, lane);
+            else warp_rule<double, false>(A, P, x, y, z, rule, lane);
             for (int q = 0; q < 9; ++q) { sl[q] = sl_entry(A, q / 3, q % 3); dl[q] = dl_entry(A, q / 3, q % 3); }
         }
         const double* f = job.f + 3 * p;
@@ -688,6 +671,15 @@ __global__ void __launch_bounds__(FIELD_WARPS * 32) field_kernel(FieldJob job) {
         job.out[3 * pt + 2] = uz;
         if (overflow) atomicExch(job.overflow, 1);
     }
+}
+
+__global__ void rsqrt_nr_kernel(int n, const double* __restrict__ x, double* __restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = rsqrt_nr(x[i]);
+}
+
+void rsqrt_nr_eval(int n, const double* x, double* y, cudaStream_t st) {
+    if (n > 0) LAUNCH(rsqrt_nr_kernel, ceil_div(n, 256), 256, 0, st, n, x, y);
 }
 
 void field_eval(const FieldJob& job, cudaStream_t st) {

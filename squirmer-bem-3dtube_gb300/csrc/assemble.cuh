@@ -96,4 +96,8 @@ constexpr int ADJ_MAX_MODES = 2;
 // Deterministic: per-CTA partials reduced in a fixed order.
 void adjoint_pairs(const AdjTerm* terms, int nterms, int nm, double* out, cudaStream_t st);
 
+// y = rsqrt_nr(x) elementwise on device arrays: the FP64 reciprocal square root of
+// the mixed path's near-singular and self integrals (for its accuracy test).
+void rsqrt_nr_eval(int n, const double* x, double* y, cudaStream_t st);
+
 }  // namespace sqbem

@@ -265,7 +265,10 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
             kstat_note(note);
         }
         if (all32) {
+            // the compensated sums are FP32-issue-bound, so the column count is a
+            // template parameter (2: refinement; 6: the rigid-body columns A_u K)
             if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<2>, grid, MV_ROWS, 0, st, a, part.get());
+            else if (maxr <= 6) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<6>, grid, MV_ROWS, 0, st, a, part.get());
             else TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
         } else if (maxr <= 2) {
             TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<2>, grid, MV_ROWS, 0, st, a, part.get());

@@ -21,9 +21,13 @@
 #include <mutex>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "mixed.cuh"
 #include "tc_gemm.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace sqbem {
 
@@ -600,13 +604,23 @@ void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------- triangular solves, few right-hand sides
-// x <- U^{-1} L^{-1} x for R <= 2 columns, one CTA per member.  The solve runs
-// by 128-row blocks: s = x_i - (off-diagonal blocks) x, by a warp per row
-// reading the row-major split factor along its contiguous index (hi + lo,
-// coalesced) against x held in shared memory; then x_i = inv(diag block) s
-// with the FP32 block inverses.  Input and output are FP64 (rows beyond n_true
-// are zero); the arithmetic is FP32 like the tensor-core solves.
+// x <- U^{-1} L^{-1} x for R <= 2 columns.  Each member is solved by a cluster
+// of TS_CL CTAs; every CTA holds all of x in its shared memory.  The solve runs
+// by 128-row blocks: s = x_b - (off-diagonal blocks) x, the block's rows split
+// over the cluster (one row per warp, reading the row-major split factor along
+// its contiguous index, hi + lo, 16 bytes per lane); each CTA writes its rows of
+// s into the shared memory of every CTA of the cluster; after the cluster
+// barrier every CTA forms x_b = inv(diag block) s itself (the 128 x 128 FP32
+// block inverse, read from L2).  s is double-buffered, so one barrier per block
+// suffices: a CTA writes block k + 1's sums only after all CTAs have reached
+// block k's barrier, i.e. have finished reading block k - 1's.  Input and output
+// are FP64 (rows beyond n_true are zero); the arithmetic is FP32 like the
+// tensor-core solves.
 constexpr int TS_THREADS = 1024;
+constexpr int TS_CL = 4;                // CTAs per member (thread-block cluster)
+constexpr int TS_ROWS = MX_NB / TS_CL;  // block rows per CTA: one per warp
+static_assert(TS_ROWS == TS_THREADS / 32, "one block row per warp");
+constexpr int TS_PARTS = TS_THREADS / MX_NB;  // the diagonal product's q range split this many ways
 struct TrsvJob {
     const bf16* Rh;
     const bf16* Rl;
@@ -623,13 +637,20 @@ struct TrsvArgs {
     TrsvJob j[MAXJOBS];
 };
 
+// shared memory of one CTA: x (n x R), s (2 x 128 x R), partial products (TS_PARTS x 128 x R)
+inline size_t trsv_smem(int n, int R) { return ((size_t)n + 2 * MX_NB + TS_PARTS * MX_NB) * R * sizeof(float); }
+
 template <int R>
-__global__ void __launch_bounds__(TS_THREADS) trsv_kernel(const __grid_constant__ TrsvArgs args) {
+__global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
+    trsv_kernel(const __grid_constant__ TrsvArgs args) {
     extern __shared__ float tsm[];
-    const TrsvJob& J = args.j[blockIdx.x];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const TrsvJob& J = args.j[blockIdx.x / TS_CL];
     const int n = args.n, nt = J.n_true, r = args.r;
-    float* x = tsm;                   // n x R, x[row * R + c]
-    float* sb = tsm + (size_t)n * R;  // 128 x R block of sums
+    float* x = tsm;                       // x[row * R + c]
+    float* sb = tsm + (size_t)n * R;      // sb[buf][rl * R + c]
+    float* part = sb + 2 * MX_NB * R;     // part[(h * 128 + rl) * R + c]
     const bf16* Rh = J.Rh;
     const bf16* Rl = J.Rl;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -639,13 +660,16 @@ __global__ void __launch_bounds__(TS_THREADS) trsv_kernel(const __grid_constant_
     }
     __syncthreads();
     const int nb = n / MX_NB;
+    int buf = 0;
     for (int pass = 0; pass < 2; ++pass) {  // 0: L (forward), 1: U (backward)
         for (int step = 0; step < nb; ++step) {
             const int b = pass == 0 ? step : nb - 1 - step;
             const int k0 = pass == 0 ? 0 : (b + 1) * MX_NB, k1 = pass == 0 ? b * MX_NB : n;
-            // s = x_b - A(b rows, [k0, k1)) x([k0, k1)): 4 rows per warp, each lane
-            // loading 8 consecutive entries (16 bytes) of hi and of lo per step
-            for (int rl = warp; rl < MX_NB; rl += TS_THREADS / 32) {
+            {
+                // s = x_b - A(row, [k0, k1)) x([k0, k1)) for this warp's row; each lane
+                // loads 8 consecutive entries of hi and of lo per step (k0, k1 and n are
+                // multiples of 128, so the 16-byte loads are aligned and in bounds)
+                const int rl = rank * TS_ROWS + warp;
                 const int row = b * MX_NB + rl;
                 float acc[R];
 #pragma unroll
@@ -669,25 +693,53 @@ __global__ void __launch_bounds__(TS_THREADS) trsv_kernel(const __grid_constant_
                     float v = acc[c];
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    if (lane == 0) sb[rl * R + c] = x[row * R + c] - v;
+                    acc[c] = x[row * R + c] - v;
+                }
+                if (lane < TS_CL) {  // lane q writes into the shared memory of cluster CTA q
+                    float* dst = cl.map_shared_rank(sb, lane) + buf * MX_NB * R + rl * R;
+#pragma unroll
+                    for (int c = 0; c < R; ++c) dst[c] = acc[c];
                 }
             }
-            __syncthreads();
-            // x_b = inv(diag block b) s   (column-major 128 x 128 FP32 inverse)
+            cl.sync();
+            // x_b = inv(diag block b) s  (column-major 128 x 128 FP32 inverse): thread
+            // (h, rl) sums q in [h * 16, h * 16 + 16), then the parts add in order h
             const float* Inv = (pass == 0 ? J.Li : J.Ui) + (size_t)b * MX_NB * MX_NB;
-            for (int e = tid; e < MX_NB * R; e += TS_THREADS) {
-                const int rl = e % MX_NB, c = e / MX_NB;
+            const float* s = sb + buf * MX_NB * R;
+            {
+                const int rl = tid % MX_NB, h = tid / MX_NB;
+                constexpr int QN = MX_NB / TS_PARTS;
+                float v[R];
+#pragma unroll
+                for (int c = 0; c < R; ++c) v[c] = 0.f;
+#pragma unroll
+                for (int q = h * QN; q < h * QN + QN; ++q) {
+                    const float a = __ldg(Inv + rl + q * MX_NB);
+#pragma unroll
+                    for (int c = 0; c < R; ++c) v[c] = fmaf(a, s[q * R + c], v[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < R; ++c) part[(h * MX_NB + rl) * R + c] = v[c];
+            }
+            __syncthreads();
+            if (tid < MX_NB * R) {
+                const int rl = tid % MX_NB, c = tid / MX_NB;
                 float v = 0.f;
-                for (int q = 0; q < MX_NB; ++q) v = fmaf(Inv[rl + q * MX_NB], sb[q * R + c], v);
+#pragma unroll
+                for (int h = 0; h < TS_PARTS; ++h) v += part[(h * MX_NB + rl) * R + c];
                 x[(b * MX_NB + rl) * R + c] = v;
             }
             __syncthreads();
+            buf ^= 1;
         }
     }
-    for (int e = tid; e < nt * R; e += TS_THREADS) {
+    // each CTA writes its share of the rows
+    for (int e = tid + rank * TS_THREADS; e < nt * R; e += TS_THREADS * TS_CL) {
         const int row = e / R, c = e % R;
         if (c < r) J.out[row + c * J.ldo] = (double)x[e];
     }
+    // no CTA leaves while a peer could still address its shared memory
+    cl.sync();
 }
 
 void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
@@ -695,7 +747,7 @@ void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const do
     if (g.empty()) return;
     if (r < 1 || r > 2) fail(SQBEM_ERR_ARG, "trsv: 1 or 2 right-hand sides");
     const int n = g[0]->n;
-    const size_t smem = ((size_t)n + MX_NB) * 2 * sizeof(float);
+    const size_t smem = trsv_smem(n, 2);
     if (smem > 227 * 1024) fail(SQBEM_ERR_ARG, "trsv: %d unknowns exceed shared memory", n);
     static std::once_flag attr;
     std::call_once(attr, [] {
@@ -714,7 +766,7 @@ void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const do
             a.j[k] = {L.Rh.get(), L.Rl.get(), L.Li.get(), L.Ui.get(), in[i0 + k], nt, out[i0 + k], nt, nt};
         }
         const double by = (double)m * ((double)n * n * 4.0 + 2.0 * n * r * 8.0);
-        TIMED_LAUNCH("trsv", 0.0, by, trsv_kernel<2>, m, TS_THREADS, smem, st, a);
+        TIMED_LAUNCH("trsv", 0.0, by, trsv_kernel<2>, m * TS_CL, TS_THREADS, smem, st, a);
     }
 }
 

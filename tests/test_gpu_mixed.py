@@ -83,3 +83,19 @@ def test_mixed_requires_mixed_tube():
     with pytest.raises(sqbem.BEMError) as e:
         sqbem.SwimmerSolver(t, sqbem.icosphere(1.0, 1), (0, 0, 0), precision=sqbem.MIXED)
     assert e.value.code == sqbem.ERR_ARG
+
+
+def test_mixed_fp64_rsqrt_error_bound():
+    """The FP64 reciprocal square root of the mixed path's near-singular and self
+    integrals (an FP32 seed and one Newton step in FP64): relative error below
+    2e-13 (1.5 e0^2 for the seed's e0 <= 2.7e-7) over the squared distances the
+    integrals meet, and far beyond them."""
+    import ctypes
+    rng = np.random.default_rng(11)
+    x = np.concatenate([10.0 ** rng.uniform(-8, 6, 200000), [1e-8, 1e-4, 0.25, 1.0, 2.0, 3.0, 1e6]])
+    y = np.zeros_like(x)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert sqbem.lib().sqbem_test_rsqrt_nr(len(x), dp(x), dp(y)) == 0
+    ref = 1.0 / np.sqrt(x)
+    err = np.abs(y - ref) / ref
+    assert err.max() < 2e-13, err.max()
