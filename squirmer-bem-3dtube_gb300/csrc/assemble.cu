@@ -268,6 +268,21 @@ __device__ void warp_self(Acc<double>& A, const PanelRec& P, double x, double y,
     warp_reduce(A);
 }
 
+// ---------------------------------------------------------------- near-pair list
+// One list of capacity near_cap: the heavy pairs (448-point rule, self
+// integral) fill it from the front, the light ones (28/112 points) from the back,
+// so the near kernel can take the heavy ones first.  near_count[0], [1]: the
+// heavy and light counts; [2]: the near kernel's work counter.  A slot is
+// written only while it is inside the list; counts whose sum exceeds the
+// capacity mean overflow (the near kernel then does nothing and the host
+// fails the call).
+template <class TO>
+__device__ __forceinline__ void near_append(const BlockJob<TO>& job, int i, int p, int rule) {
+    const bool heavy = rule >= 3;
+    const int slot = atomicAdd(job.near_count + (heavy ? 0 : 1), 1);
+    if (slot < job.near_cap) job.near_list[heavy ? slot : job.near_cap - 1 - slot] = make_int2(i, p | (rule << 28));
+}
+
 // ---------------------------------------------------------------- far kernel
 constexpr int FAR_TGT = 64;   // targets per CTA (threads)
 constexpr int FAR_SRC = 16;   // source panels per CTA
@@ -339,8 +354,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
         if constexpr (sizeof(TC) == 8) {
             const int rule = self ? 4 : rule_of(P, x, y, z);
             if (rule != 0) {
-                const int slot = atomicAdd(job.near_count, 1);
-                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
+                near_append(job, i, p, rule);
                 continue;
             }
             const double e0x = P.v[0] - x, e0y = P.v[1] - y, e0z = P.v[2] - z;
@@ -374,8 +388,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
                 if (!(d2 > F.far2 * (1.0 + 1e-12))) rule = rule_of(P, x, y, z);
             }
             if (rule != 0) {
-                const int slot = atomicAdd(job.near_count, 1);
-                if (slot < job.near_cap) job.near_list[slot] = make_int2(i, p | (rule << 28));
+                near_append(job, i, p, rule);
                 continue;
             }
             // r = (c - x0) + sum_k l_k (V_k - c)
@@ -400,14 +413,22 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
 }
 
 // ---------------------------------------------------------------- near kernel
+// Warps take pairs from a shared counter, heavy pairs first (a heavy pair costs
+// up to 16x a light one; static striding left SMs idle for a third of the run).
+// Each pair is computed whole by one warp, so the result does not depend on the
+// order.
 template <class TO, bool MIXED>
-__global__ void __launch_bounds__(256) near_kernel(BlockJob<TO> job) {
+__global__ void __launch_bounds__(256, 3) near_kernel(BlockJob<TO> job) {
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int count = min(*job.near_count, job.near_cap);
-    for (int k = warp; k < count; k += nwarps) {
-        const int2 e = job.near_list[k];
+    const int nh = job.near_count[0], nl = job.near_count[1];
+    if (nh + nl > job.near_cap) return;  // overflow: reported by the host
+    const int count = nh + nl;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(job.near_count + 2, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= count) break;
+        const int2 e = job.near_list[k < nh ? k : job.near_cap - 1 - (k - nh)];
         const int i = e.x, p = e.y & 0x0fffffff;
         const PanelRec P = job.src[p];
         const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
@@ -441,7 +462,7 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     init_tables();
     BlockJob<TO> job = job0;
     DevBuf<int2> list((size_t)near_cap, st);
-    DevBuf<int> count(1, st);
+    DevBuf<int> count(3, st);
     count.zero();
     job.near_list = list.get();
     job.near_count = count.get();
@@ -453,7 +474,14 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     const double by = pairs * 9.0 * sizeof(TO) * ((job.S ? 1 : 0) + (job.D ? 1 : 0));
     if (mixed) TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
     else TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
-    const int warps = 152 * 16;
+    static int sms = 0;
+    static std::once_flag sms_once;
+    std::call_once(sms_once, [] {
+        int dev = 0;
+        CUDA_CHECK(cudaGetDevice(&dev));
+        CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    });
+    const int warps = sms * 24;  // 3 CTAs of 8 warps per SM (80 registers per thread)
     if (kstats_on()) {
         char note[96];
         std::snprintf(note, sizeof note, "nT=%d nS=%d same=%d mixed=%d", job.nT, job.nS, job.same_mesh, (int)mixed);
@@ -463,10 +491,11 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     else TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
     if ((long long)job.nT * job.nS > near_cap) {
         // the list could overflow only for blocks larger than its capacity
-        int h = 0;
-        count.download(&h, 1);
+        int h[3] = {};
+        count.download(h, 3);
         CUDA_CHECK(cudaStreamSynchronize(st));
-        if (h > near_cap) fail(SQBEM_ERR_ARG, "near-pair list overflow (%d > %d)", h, near_cap);
+        if ((long long)h[0] + h[1] > near_cap)
+            fail(SQBEM_ERR_ARG, "near-pair list overflow (%lld > %d)", (long long)h[0] + h[1], near_cap);
     }
 }
 

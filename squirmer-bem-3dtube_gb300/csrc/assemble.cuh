@@ -36,7 +36,7 @@ struct BlockJob {
     long long d_rs = 1, d_cs = 0;
     double sscale = 0, dscale = 0;
     int2* near_list = nullptr;
-    int* near_count = nullptr;
+    int* near_count = nullptr;  // [heavy, light, work counter] (assemble.cu)
     int near_cap = 0;
 };
 
