@@ -31,6 +31,7 @@
 // FP64, with a reciprocal square root refined from an FP32 seed (rsqrt_nr).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -287,32 +288,11 @@ __device__ __forceinline__ void near_append(const BlockJob<TO>& job, int i, int 
 constexpr int FAR_TGT = 64;   // targets per CTA (threads)
 constexpr int FAR_SRC = 16;   // source panels per CTA
 
-// FP32 view of a source panel for the mixed far field: vertex offsets from the
-// centroid (exact in FP64, rounded once), normal, area, the centroid as an
-// unevaluated sum hi + lo of two floats, and the squared far-field radius
-// (3 h)^2: in FP64 for the exact test and, raised by 1e-5, in FP32 for the
-// quick one.
-struct FarF {
-    float d[9];
-    float n[3];
-    float area;
-    float far2f;
-    float chi[3], clo[3];
-    double far2;
-};
-
-// v = hi + lo with hi = fl32(v) and lo = fl32(v - hi): the pair carries v to
-// about 2^-48 relative, so a difference of two such pairs formed in FP32,
-// (a_hi - b_hi) + (a_lo - b_lo), is within ~2.5 FP32 ulps of the exact one.
-__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
-
-template <class TO, class TC>
+// FP64 mode: one thread per target, the CTA's source panels staged in shared
+// memory; the exact rule test per pair, then the 7-point rule in FP64.
+template <class TO>
 __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
     __shared__ PanelRec sp[FAR_SRC];
-    __shared__ FarF sf[FAR_SRC];
     const int p0 = blockIdx.y * FAR_SRC;
     const int ns = min(FAR_SRC, job.nS - p0);
     {
@@ -322,84 +302,142 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
         for (int k = threadIdx.x; k < nd; k += blockDim.x) dst[k] = src[k];
     }
     __syncthreads();
-    if constexpr (sizeof(TC) == 4) {
-        if (threadIdx.x < ns) {
-            const PanelRec& P = sp[threadIdx.x];
-            FarF& F = sf[threadIdx.x];
-            for (int k = 0; k < 9; ++k) F.d[k] = (float)(P.v[k] - P.c[k % 3]);
-            F.n[0] = (float)P.n[0]; F.n[1] = (float)P.n[1]; F.n[2] = (float)P.n[2];
-            F.area = (float)P.area;
-            F.far2 = 9.0 * P.h * P.h;
-            F.far2f = (float)(F.far2 * (1.0 + 1e-5));
-            for (int k = 0; k < 3; ++k) split2(P.c[k], F.chi[k], F.clo[k]);
-        }
-        __syncthreads();
-    }
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     if (i >= job.nT) return;
     const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
-    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
-    if constexpr (sizeof(TC) == 4) {
-        split2(x, xh, xl);
-        split2(y, yh, yl);
-        split2(z, zh, zl);
-    }
-    const TC ss = (TC)job.sscale, ds = (TC)job.dscale;
     for (int s = 0; s < ns; ++s) {
         const PanelRec& P = sp[s];
         const int p = p0 + s;
-        const bool self = job.same_mesh && p == i;
-        Acc<TC> A;
+        const int rule = (job.same_mesh && p == i) ? 4 : rule_of(P, x, y, z);
+        if (rule != 0) {
+            near_append(job, i, p, rule);
+            continue;
+        }
+        Acc<double> A;
         A.zero();
-        if constexpr (sizeof(TC) == 8) {
-            const int rule = self ? 4 : rule_of(P, x, y, z);
-            if (rule != 0) {
-                near_append(job, i, p, rule);
-                continue;
-            }
-            const double e0x = P.v[0] - x, e0y = P.v[1] - y, e0z = P.v[2] - z;
-            const double e1x = P.v[3] - x, e1y = P.v[4] - y, e1z = P.v[5] - z;
-            const double e2x = P.v[6] - x, e2y = P.v[7] - y, e2z = P.v[8] - z;
-            const double mx = P.n[0], my = P.n[1], mz = P.n[2], area = P.area;
+        const double e0x = P.v[0] - x, e0y = P.v[1] - y, e0z = P.v[2] - z;
+        const double e1x = P.v[3] - x, e1y = P.v[4] - y, e1z = P.v[5] - z;
+        const double e2x = P.v[6] - x, e2y = P.v[7] - y, e2z = P.v[8] - z;
+        const double mx = P.n[0], my = P.n[1], mz = P.n[2], area = P.area;
 #pragma unroll
-            for (int q = 0; q < 7; ++q) {
-                const double l0 = c_rule7[q].l0, l1 = c_rule7[q].l1, l2 = c_rule7[q].l2, w = c_rule7[q].w;
-                accum<double, true>(A, l0 * e0x + l1 * e1x + l2 * e2x, l0 * e0y + l1 * e1y + l2 * e2y,
-                                    l0 * e0z + l1 * e1z + l2 * e2z, w * area, mx, my, mz);
-            }
-        } else {
-            // c - x0 from the hi + lo pairs (relative error <= ~2.5 ulp per
-            // component, so d2 is within ~5e-7 of the exact value).  A pair is far
-            // without further test when d2 clears (3 h)^2 by 1e-5; otherwise the
-            // FP64 test on the squared distance decides, and the reference's exact
-            // test (sqrt, division) runs inside a +-1e-12 band around the threshold
-            // and for every near pair -- the same rule as a pure FP64 decision.
-            const FarF& F = sf[s];
-            const float bx = (F.chi[0] - xh) + (F.clo[0] - xl);
-            const float by = (F.chi[1] - yh) + (F.clo[1] - yl);
-            const float bz = (F.chi[2] - zh) + (F.clo[2] - zl);
-            int rule = 0;
-            if (self) {
-                rule = 4;
-            } else if (!(bx * bx + by * by + bz * bz > F.far2f)) {
-                const double cx = P.c[0] - x, cy = P.c[1] - y, cz = P.c[2] - z;
-                const double d2 = cx * cx + cy * cy + cz * cz;
-                // the near kernel takes the exact rule from the list
-                if (!(d2 > F.far2 * (1.0 + 1e-12))) rule = rule_of(P, x, y, z);
-            }
-            if (rule != 0) {
-                near_append(job, i, p, rule);
-                continue;
-            }
-            // r = (c - x0) + sum_k l_k (V_k - c)
+        for (int q = 0; q < 7; ++q) {
+            const double l0 = c_rule7[q].l0, l1 = c_rule7[q].l1, l2 = c_rule7[q].l2, w = c_rule7[q].w;
+            accum<double, true>(A, l0 * e0x + l1 * e1x + l2 * e2x, l0 * e0y + l1 * e1y + l2 * e2y,
+                                l0 * e0z + l1 * e1z + l2 * e2z, w * area, mx, my, mz);
+        }
 #pragma unroll
-            for (int q = 0; q < 7; ++q) {
-                const float l0 = c_rule7f[q].l0, l1 = c_rule7f[q].l1, l2 = c_rule7f[q].l2, w = c_rule7f[q].w;
-                const float rx = bx + (l0 * F.d[0] + l1 * F.d[3] + l2 * F.d[6]);
-                const float ry = by + (l0 * F.d[1] + l1 * F.d[4] + l2 * F.d[7]);
-                const float rz = bz + (l0 * F.d[2] + l1 * F.d[5] + l2 * F.d[8]);
-                accum<float, true>(A, rx, ry, rz, w * F.area, F.n[0], F.n[1], F.n[2]);
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const long long r = 3LL * i + a, c = 3LL * p + b;
+                if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)(sl_entry(A, a, b) * job.sscale);
+                if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)(dl_entry(A, a, b) * job.dscale);
             }
+    }
+}
+
+// FP32 view of a source panel for the mixed far field, formed once per block by
+// far_prep_kernel: vertex offsets from the centroid (exact in FP64, rounded
+// once), normal, area, the centroid as an unevaluated sum hi + lo of two
+// floats, and the squared rule thresholds (0.75 h)^2, (1.5 h)^2, (3 h)^2 lowered
+// (thlo) and raised (thhi) by 1e-5.
+struct __align__(16) FarF {
+    float d[9];
+    float n[3];
+    float area;
+    float chi[3], clo[3];
+    float thlo[3], thhi[3];
+    float pad[3];
+};
+static_assert(sizeof(FarF) % 16 == 0, "FarF is copied as float4");
+
+// v = hi + lo with hi = fl32(v) and lo = fl32(v - hi): the pair carries v to
+// about 2^-48 relative, so a difference of two such pairs formed in FP32,
+// (a_hi - b_hi) + (a_lo - b_lo), is within ~2.5 FP32 ulps of the exact one.
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// FarF of every source panel and the hi + lo split (x, y, z hi; x, y, z lo) of
+// every target: the only FP64 work of the mixed far field.
+__global__ void far_prep_kernel(const PanelRec* __restrict__ src, int nS, const double* __restrict__ tgt, int nT,
+                                FarF* __restrict__ srcf, float* __restrict__ tgtf) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nS) {
+        const PanelRec& P = src[k];
+        FarF F;
+        for (int q = 0; q < 9; ++q) F.d[q] = (float)(P.v[q] - P.c[q % 3]);
+        for (int q = 0; q < 3; ++q) {
+            F.n[q] = (float)P.n[q];
+            split2(P.c[q], F.chi[q], F.clo[q]);
+        }
+        F.area = (float)P.area;
+        const double h2 = P.h * P.h;
+        const double t[3] = {0.5625 * h2, 2.25 * h2, 9.0 * h2};
+        for (int q = 0; q < 3; ++q) {
+            F.thlo[q] = (float)(t[q] * (1.0 - 1e-5));
+            F.thhi[q] = (float)(t[q] * (1.0 + 1e-5));
+            F.pad[q] = 0.f;
+        }
+        srcf[k] = F;
+    }
+    if (k < nT)
+        for (int q = 0; q < 3; ++q) split2(tgt[3 * k + q], tgtf[6 * k + q], tgtf[6 * k + 3 + q]);
+}
+
+// Mixed mode: as far_kernel, all in FP32.  c - x0 comes from the hi + lo pairs
+// (relative error <= ~2.5 ulp per component, so d2 is within ~5e-7 of the exact
+// value), and the rule from comparing d2 with the thresholds' 1e-5 bands: a
+// pair clear of every band has the rule the reference's FP64 test gives; a
+// pair inside a band (rare) takes the reference's exact test (rule_of).  The
+// near kernel takes the rule from the list.
+template <class TO>
+__global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, const FarF* __restrict__ srcf,
+                                                          const float* __restrict__ tgtf) {
+    __shared__ FarF sf[FAR_SRC];
+    const int p0 = blockIdx.y * FAR_SRC;
+    const int ns = min(FAR_SRC, job.nS - p0);
+    {
+        const float4* s4 = reinterpret_cast<const float4*>(srcf + p0);
+        float4* d4 = reinterpret_cast<float4*>(sf);
+        const int n4 = ns * (int)(sizeof(FarF) / sizeof(float4));
+        for (int k = threadIdx.x; k < n4; k += blockDim.x) d4[k] = s4[k];
+    }
+    __syncthreads();
+    const int i = blockIdx.x * FAR_TGT + threadIdx.x;
+    if (i >= job.nT) return;
+    const float xh = tgtf[6 * i], yh = tgtf[6 * i + 1], zh = tgtf[6 * i + 2];
+    const float xl = tgtf[6 * i + 3], yl = tgtf[6 * i + 4], zl = tgtf[6 * i + 5];
+    const float ss = (float)job.sscale, ds = (float)job.dscale;
+    for (int s = 0; s < ns; ++s) {
+        const FarF& F = sf[s];
+        const int p = p0 + s;
+        const float bx = (F.chi[0] - xh) + (F.clo[0] - xl);
+        const float by = (F.chi[1] - yh) + (F.clo[1] - yl);
+        const float bz = (F.chi[2] - zh) + (F.clo[2] - zl);
+        const float d2 = bx * bx + by * by + bz * bz;
+        int rule;
+        if (job.same_mesh && p == i) rule = 4;
+        else if (d2 > F.thhi[2]) rule = 0;
+        else if (d2 < F.thlo[2] && d2 > F.thhi[1]) rule = 1;
+        else if (d2 < F.thlo[1] && d2 > F.thhi[0]) rule = 2;
+        else if (d2 < F.thlo[0]) rule = 3;
+        else rule = rule_of(job.src[p], job.tgt[3 * i], job.tgt[3 * i + 1], job.tgt[3 * i + 2]);
+        if (rule != 0) {
+            near_append(job, i, p, rule);
+            continue;
+        }
+        Acc<float> A;
+        A.zero();
+        // r = (c - x0) + sum_k l_k (V_k - c)
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            const float l0 = c_rule7f[q].l0, l1 = c_rule7f[q].l1, l2 = c_rule7f[q].l2, w = c_rule7f[q].w;
+            const float rx = bx + (l0 * F.d[0] + l1 * F.d[3] + l2 * F.d[6]);
+            const float ry = by + (l0 * F.d[1] + l1 * F.d[4] + l2 * F.d[7]);
+            const float rz = bz + (l0 * F.d[2] + l1 * F.d[5] + l2 * F.d[8]);
+            accum<float, true>(A, rx, ry, rz, w * F.area, F.n[0], F.n[1], F.n[2]);
         }
 #pragma unroll
         for (int b = 0; b < 3; ++b)
@@ -472,8 +510,15 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     const double pairs = (double)job.nT * job.nS;
     const double fl = pairs * 7.0 * FLOPS_PER_EVAL;
     const double by = pairs * 9.0 * sizeof(TO) * ((job.S ? 1 : 0) + (job.D ? 1 : 0));
-    if (mixed) TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, float>), grid, FAR_TGT, 0, st, job);
-    else TIMED_LAUNCH("assemble_far", fl, by, (far_kernel<TO, double>), grid, FAR_TGT, 0, st, job);
+    if (mixed) {
+        DevBuf<FarF> srcf((size_t)job.nS, st);
+        DevBuf<float> tgtf((size_t)job.nT * 6, st);
+        LAUNCH(far_prep_kernel, ceil_div(std::max(job.nS, job.nT), 128), 128, 0, st, job.src, job.nS, job.tgt, job.nT,
+               srcf.get(), tgtf.get());
+        TIMED_LAUNCH("assemble_far", fl, by, far_kernel_f32<TO>, grid, FAR_TGT, 0, st, job, srcf.get(), tgtf.get());
+    } else {
+        TIMED_LAUNCH("assemble_far", fl, by, far_kernel<TO>, grid, FAR_TGT, 0, st, job);
+    }
     static int sms = 0;
     static std::once_flag sms_once;
     std::call_once(sms_once, [] {

@@ -583,23 +583,63 @@ void lu_rec(const std::vector<MixedLU*>& g, int c0, int w, const MixedCtx& cx) {
 
 }  // namespace
 
+// Column-major to column-major (no transposition), every pointer and column
+// stride allowing 16-byte FP32 and 8-byte BF16 vectors, rows a multiple of 4:
+// one thread per 4 rows of a column, no shared memory.
+__global__ void __launch_bounds__(256) conv_direct_kernel(const __grid_constant__ ConvArgs args) {
+    const ConvJob& J = args.j[blockIdx.y];
+    const int r4 = J.rows / 4;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= r4 * J.cols) return;
+    const int c = t / r4, r = (t - c * r4) * 4;
+    const float4 v = *reinterpret_cast<const float4*>(J.src + r + (long long)c * J.s_cs);
+    const float x[4] = {v.x, v.y, v.z, v.w};
+    uint2 hv, lv;
+    bf16* hp = reinterpret_cast<bf16*>(&hv);
+    bf16* lp = reinterpret_cast<bf16*>(&lv);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const bf16 h = __float2bfloat16_rn(x[q]);
+        hp[q] = h;
+        lp[q] = __float2bfloat16_rn(x[q] - __bfloat162float(h));
+    }
+    const long long o = r + (long long)c * J.d_cs;
+    *reinterpret_cast<uint2*>(J.hi + o) = hv;
+    *reinterpret_cast<uint2*>(J.lo + o) = lv;
+}
+
+namespace {
+bool direct_ok(const ConvJob& j) {
+    return j.s_rs == 1 && j.d_rs == 1 && j.rows % 4 == 0 && j.s_cs % 4 == 0 && j.d_cs % 4 == 0 &&
+           ((uintptr_t)j.src & 15) == 0 && ((uintptr_t)j.hi & 7) == 0 && ((uintptr_t)j.lo & 7) == 0 &&
+           (long long)(j.rows / 4) * j.cols <= 0x7fffffffLL;
+}
+}  // namespace
+
 void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st) {
     if (jobs.empty()) return;
     for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
         ConvArgs a;
         a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
-        long long mx = 0;
+        long long mx = 0, mxd = 0;
         double bytes = 0;
+        bool direct = true;
         for (int k = 0; k < a.n; ++k) {
             a.j[k] = jobs[i0 + k];
             const long long tiles = (long long)((a.j[k].rows + CV_T - 1) / CV_T) * ((a.j[k].cols + CV_T - 1) / CV_T);
             mx = std::max(mx, tiles);
+            mxd = std::max(mxd, (long long)(a.j[k].rows / 4) * a.j[k].cols);
+            direct = direct && direct_ok(a.j[k]);
             bytes += 8.0 * a.j[k].rows * a.j[k].cols;  // FP32 read, two BF16 written
         }
         if (mx == 0) continue;
         if (mx > 0x7fffffffLL) fail(SQBEM_ERR_ARG, "convert: block too large");
-        TIMED_LAUNCH("convert", 0.0, bytes, conv_kernel, dim3((unsigned)mx, (unsigned)a.n), dim3(CV_T, CV_RY), 0, st,
-                     a);
+        if (direct)
+            TIMED_LAUNCH("convert", 0.0, bytes, conv_direct_kernel, dim3((unsigned)ceil_div(mxd, 256), (unsigned)a.n),
+                         256, 0, st, a);
+        else
+            TIMED_LAUNCH("convert", 0.0, bytes, conv_kernel, dim3((unsigned)mx, (unsigned)a.n), dim3(CV_T, CV_RY), 0,
+                         st, a);
     }
 }
 

@@ -326,7 +326,9 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
                 if (Tt.explicit_inverse()) fail(SQBEM_ERR_ARG, "mixed swimmers of one group share a tube mode");
                 const int ntp = Tt.ntp;
                 yp[k].alloc((size_t)ntp * M.nc, cx.st);
-                yp[k].zero();
+                if (ntp > M.nt)  // rows nt .. ntp of every column; the copies below fill the rest
+                    CUDA_CHECK(cudaMemset2DAsync(yp[k].get() + M.nt, sizeof(float) * ntp, 0,
+                                                 sizeof(float) * (ntp - M.nt), M.nc, cx.st));
                 cj.push_back(cp32_32(M.B.get(), M.nt, yp[k].get(), ntp, M.nt, M.ns));
                 cj.push_back(cp32_32(M.Ct.get(), M.nt, yp[k].get() + (size_t)ntp * M.ns, ntp, M.nt, 6));
                 tl.push_back(Tt.lu.get());
@@ -336,19 +338,18 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             copy_group(cj, cx.st);
             cj.clear();
             mixed_lu_solve(tl, rhs, cx);
-            for (size_t k = 0; k < G; ++k) {
+            for (size_t k = 0; k < G; ++k) {  // Y stays in the padded buffer
                 MixedSwimmer& M = sw[k]->mx;
-                M.Y.alloc((size_t)M.nt * M.nc, cx.st);
-                cj.push_back(cp32_32(yp[k].get(), sw[k]->tube->mt.ntp, M.Y.get(), M.nt, M.nt, M.nc));
+                M.Y = std::move(yp[k]);
+                M.ldY = sw[k]->tube->mt.ntp;
             }
-            copy_group(cj, cx.st);
-            cj.clear();
         }
         for (size_t k = 0; k < G && sw[0]->tube->mt.explicit_inverse(); ++k) {
             MixedSwimmer& M = sw[k]->mx;
             const MixedTube& Tt = sw[k]->tube->mt;
             const int ntp = Tt.ntp;
             M.Y.alloc((size_t)M.nt * M.nc, cx.st);
+            M.ldY = M.nt;
             TcProblem p;
             p.M = M.nt; p.N = M.nc; p.K = M.nt; p.alpha = 1.f; p.beta = 0.f;
             p.C = M.Y.get(); p.c_rs = 1; p.c_cs = M.nt;
@@ -612,7 +613,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             cj.clear();
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                mj.push_back(mv32(M.Y.get(), M.nt, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
+                mj.push_back(mv32(M.Y.get(), M.ldY, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();

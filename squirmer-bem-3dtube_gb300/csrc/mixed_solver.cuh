@@ -5,11 +5,12 @@
 //   [ D  E  Cs ] [f_s] = [b_s]        b_s = -A_uBs u_s
 //   [ 0  F  0  ] [ w ]   [ 0 ]        F: force-free / torque-free rows
 // Blocks are assembled in FP32 and kept for the FP64 residual.  The
-// preconditioner is the Schur elimination on split-BF16 tensor cores:
-// T^{-1} (LU of T, then the LU solve of the identity), Y = T^{-1}[B | Ct] as one
-// GEMM, G = [E | Cs] - D Y, G_s^{-1} the same way, Z = G_s^{-1} G_c and the
-// 6 x 6 rigid-body system S6 = F Z solved in FP64.  With the two inverses held
-// explicitly, every refinement step is a handful of HBM-bound products.
+// preconditioner is the Schur elimination on split-BF16 tensor cores: the LU of
+// T; Y = T^{-1}[B | Ct] by the LU solves (a tube serving one swimmer) or as one
+// GEMM with an explicit T^{-1} (a tube shared by many swimmers); G = [E | Cs] -
+// D Y, G_s^{-1} formed explicitly, Z = G_s^{-1} G_c and the 6 x 6 rigid-body
+// system S6 = F Z solved in FP64.  Every refinement step is one triangular solve
+// with T's factor (or a product with T^{-1}) and a handful of HBM-bound products.
 // Iterative refinement on the full system, residuals accumulated in FP64,
 // stops when the relative residual reaches REFINE_TOL.
 #pragma once
@@ -52,7 +53,8 @@ struct MixedSwimmer {
     DevBuf<float> D;              // ns x nt
     DevBuf<float> E, AuBs;        // ns x ns
     DevBuf<float> Ct, Cs;         // nt x 6, ns x 6
-    DevBuf<float> Y;              // T^{-1} [B | Ct], nt x nc (ld nt)
+    DevBuf<float> Y;              // T^{-1} [B | Ct], nt x nc, leading dimension ldY
+    long long ldY = 0;            // nt (explicit T^{-1}) or the padded ntp (the LU solve's buffer)
     DevBuf<float> Gi;             // G_s^{-1}, nsp x nsp column-major
     DevBuf<double> Z64;           // G_s^{-1} G_c (ns x 6), FP64
     DevBuf<double> F;             // 6 x ns, column-major (ld 6), unscaled
