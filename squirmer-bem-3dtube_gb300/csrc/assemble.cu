@@ -391,11 +391,17 @@ __global__ void far_prep_kernel(const PanelRec* __restrict__ src, int nS, const 
 // value), and the rule from comparing d2 with the thresholds' 1e-5 bands: a
 // pair clear of every band has the rule the reference's FP64 test gives; a
 // pair inside a band (rare) takes the reference's exact test (rule_of).  The
-// near kernel takes the rule from the list.
+// near kernel takes the rule from the list.  Near pairs are gathered in a
+// shared-memory list first (heavy from the front, light from the back) and
+// appended to the global list with one atomic per class at the end of the CTA,
+// so no thread waits on a global atomic inside the pair loop.
+constexpr int FAR_PAIRS = FAR_TGT * FAR_SRC;
 template <class TO>
 __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, const FarF* __restrict__ srcf,
                                                           const float* __restrict__ tgtf) {
     __shared__ FarF sf[FAR_SRC];
+    __shared__ int2 nl[FAR_PAIRS];
+    __shared__ int ncount[2], nbase[2];
     const int p0 = blockIdx.y * FAR_SRC;
     const int ns = min(FAR_SRC, job.nS - p0);
     {
@@ -404,13 +410,17 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         const int n4 = ns * (int)(sizeof(FarF) / sizeof(float4));
         for (int k = threadIdx.x; k < n4; k += blockDim.x) d4[k] = s4[k];
     }
+    if (threadIdx.x < 2) ncount[threadIdx.x] = 0;
     __syncthreads();
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
-    if (i >= job.nT) return;
-    const float xh = tgtf[6 * i], yh = tgtf[6 * i + 1], zh = tgtf[6 * i + 2];
-    const float xl = tgtf[6 * i + 3], yl = tgtf[6 * i + 4], zl = tgtf[6 * i + 5];
+    const int nsi = i < job.nT ? ns : 0;  // targets past the end take part in the barriers only
+    float xh = 0.f, yh = 0.f, zh = 0.f, xl = 0.f, yl = 0.f, zl = 0.f;
+    if (nsi > 0) {
+        xh = tgtf[6 * i]; yh = tgtf[6 * i + 1]; zh = tgtf[6 * i + 2];
+        xl = tgtf[6 * i + 3]; yl = tgtf[6 * i + 4]; zl = tgtf[6 * i + 5];
+    }
     const float ss = (float)job.sscale, ds = (float)job.dscale;
-    for (int s = 0; s < ns; ++s) {
+    for (int s = 0; s < nsi; ++s) {
         const FarF& F = sf[s];
         const int p = p0 + s;
         const float bx = (F.chi[0] - xh) + (F.clo[0] - xl);
@@ -425,7 +435,9 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         else if (d2 < F.thlo[0]) rule = 3;
         else rule = rule_of(job.src[p], job.tgt[3 * i], job.tgt[3 * i + 1], job.tgt[3 * i + 2]);
         if (rule != 0) {
-            near_append(job, i, p, rule);
+            const bool heavy = rule >= 3;
+            const int slot = atomicAdd(&ncount[heavy ? 0 : 1], 1);  // at most FAR_PAIRS in total
+            nl[heavy ? slot : FAR_PAIRS - 1 - slot] = make_int2(i, p | (rule << 28));
             continue;
         }
         Acc<float> A;
@@ -447,6 +459,21 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
                 if (job.S) job.S[r * job.s_rs + c * job.s_cs] = (TO)(sl_entry(A, a, b) * ss);
                 if (job.D) job.D[r * job.d_rs + c * job.d_cs] = (TO)(dl_entry(A, a, b) * ds);
             }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        const int n = ncount[threadIdx.x];
+        nbase[threadIdx.x] = n > 0 ? atomicAdd(job.near_count + threadIdx.x, n) : 0;
+    }
+    __syncthreads();
+    const int nh = ncount[0], nlt = ncount[1], cap = job.near_cap;
+    for (int e = threadIdx.x; e < nh; e += FAR_TGT) {
+        const int slot = nbase[0] + e;
+        if (slot < cap) job.near_list[slot] = nl[e];
+    }
+    for (int e = threadIdx.x; e < nlt; e += FAR_TGT) {
+        const int slot = nbase[1] + e;
+        if (slot < cap) job.near_list[cap - 1 - slot] = nl[FAR_PAIRS - 1 - e];
     }
 }
 
