@@ -677,8 +677,16 @@ struct TrsvArgs {
     TrsvJob j[MAXJOBS];
 };
 
-// shared memory of one CTA: x (n x R), s (2 x 128 x R), partial products (TS_PARTS x 128 x R)
-inline size_t trsv_smem(int n, int R) { return ((size_t)n + 2 * MX_NB + TS_PARTS * MX_NB) * R * sizeof(float); }
+// x lives in shared memory per column, at position xpos(k): lane l of a warp
+// reads entries k0 + 8 l + q (q = 0..7) of its row's 8-column segment, so entry k
+// goes to (k & ~255) + 32 (k & 7) + ((k >> 3) & 31) -- the 32 lanes hit 32
+// consecutive words (no bank conflict).  Columns are padded to a multiple of 256.
+__device__ __forceinline__ int xpos(int k) { return (k & ~255) + ((k & 7) << 5) + ((k >> 3) & 31); }
+inline int trsv_npad(int n) { return (n + 255) & ~255; }
+// shared memory of one CTA: x (npad x R), s (2 x 128 x R), partial products (TS_PARTS x 128 x R)
+inline size_t trsv_smem(int n, int R) {
+    return ((size_t)trsv_npad(n) + 2 * MX_NB + TS_PARTS * MX_NB) * R * sizeof(float);
+}
 
 template <int R>
 __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
@@ -688,15 +696,16 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
     const int rank = (int)cl.block_rank();
     const TrsvJob& J = args.j[blockIdx.x / TS_CL];
     const int n = args.n, nt = J.n_true, r = args.r;
-    float* x = tsm;                       // x[row * R + c]
-    float* sb = tsm + (size_t)n * R;      // sb[buf][rl * R + c]
-    float* part = sb + 2 * MX_NB * R;     // part[(h * 128 + rl) * R + c]
+    const int npad = (n + 255) & ~255;
+    float* x = tsm;                        // column c: x[c * npad + xpos(row)]
+    float* sb = tsm + (size_t)npad * R;    // sb[buf][rl * R + c]
+    float* part = sb + 2 * MX_NB * R;      // part[(h * 128 + rl) * R + c]
     const bf16* Rh = J.Rh;
     const bf16* Rl = J.Rl;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int e = tid; e < n * R; e += TS_THREADS) {
         const int row = e / R, c = e % R;
-        x[e] = (row < nt && c < r) ? (float)J.in[row + c * J.ldi] : 0.f;
+        x[c * npad + xpos(row)] = (row < nt && c < r) ? (float)J.in[row + c * J.ldi] : 0.f;
     }
     __syncthreads();
     const int nb = n / MX_NB;
@@ -721,11 +730,12 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
                     const uint4 lv = *reinterpret_cast<const uint4*>(Rl + base + k);
                     const bf16* hp = reinterpret_cast<const bf16*>(&hv);
                     const bf16* lp = reinterpret_cast<const bf16*>(&lv);
+                    const int xp = xpos(k);  // k is a multiple of 8: entry k + q sits at xp + 32 q
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
                         const float a = __bfloat162float(hp[q]) + __bfloat162float(lp[q]);
 #pragma unroll
-                        for (int c = 0; c < R; ++c) acc[c] = fmaf(a, x[(k + q) * R + c], acc[c]);
+                        for (int c = 0; c < R; ++c) acc[c] = fmaf(a, x[c * npad + xp + 32 * q], acc[c]);
                     }
                 }
 #pragma unroll
@@ -733,7 +743,7 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
                     float v = acc[c];
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    acc[c] = x[row * R + c] - v;
+                    acc[c] = x[c * npad + xpos(row)] - v;
                 }
                 if (lane < TS_CL) {  // lane q writes into the shared memory of cluster CTA q
                     float* dst = cl.map_shared_rank(sb, lane) + buf * MX_NB * R + rl * R;
@@ -767,7 +777,7 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
                 float v = 0.f;
 #pragma unroll
                 for (int h = 0; h < TS_PARTS; ++h) v += part[(h * MX_NB + rl) * R + c];
-                x[(b * MX_NB + rl) * R + c] = v;
+                x[c * npad + xpos(b * MX_NB + rl)] = v;
             }
             __syncthreads();
             buf ^= 1;
@@ -776,7 +786,7 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
     // each CTA writes its share of the rows
     for (int e = tid + rank * TS_THREADS; e < nt * R; e += TS_THREADS * TS_CL) {
         const int row = e / R, c = e % R;
-        if (c < r) J.out[row + c * J.ldo] = (double)x[e];
+        if (c < r) J.out[row + c * J.ldo] = (double)x[c * npad + xpos(row)];
     }
     // no CTA leaves while a peer could still address its shared memory
     cl.sync();
