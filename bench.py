@@ -18,9 +18,9 @@ Per-instance working sets (dense blocks of 3N x 3N) exceed the 129 MB L2, so no
 explicit L2 flush is done between steps.
 
 --impl reference times the reference algorithm on the host cores instead: the
-oracle's CPU restatement (C assembly, as single-threaded as the reference's,
-plus LAPACK through scipy on all cores), on a bounded sample of the same
-workload per step.
+oracle's CPU restatement (C assembly plus LAPACK through scipy) on every core,
+one process per core with single-threaded BLAS, each step one instance per
+process from the same workload.
 """
 import argparse
 import json
@@ -219,23 +219,91 @@ def cpu_sample(insts, budget_s=20.0):
     return done, dt, levels
 
 
+BLAS_THREAD_VARS = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+def _cpu_init():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    orc.lib()
+
+
+def _cpu_wait(seconds):
+    time.sleep(seconds)
+    return 0
+
+
+def _cpu_worker(inst):
+    """One instance through the oracle in a pool process."""
+    import oracle as orc
+    cpu_solve(orc, inst)
+    return inst["sphere_level"]
+
+
+class CpuPool:
+    """The reference algorithm's throughput on all host cores: one spawned
+    process per core, whole instances each, BLAS on one thread per process
+    (independent solves, as the instances of a sweep are)."""
+
+    def __init__(self):
+        import multiprocessing as mp
+        _cpu_init()  # builds the oracle here if needed, before the workers load it
+        self.n = os.cpu_count() or 1
+        saved = {k: os.environ.get(k) for k in BLAS_THREAD_VARS}
+        for k in BLAS_THREAD_VARS:
+            os.environ[k] = "1"  # read by the children's BLAS at load time
+        try:
+            self.pool = mp.get_context("spawn").Pool(self.n, initializer=_cpu_init)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        self.pool.map(_cpu_wait, [0.5] * self.n, chunksize=1)  # every worker up and loaded
+
+    def run(self, insts):
+        t0 = time.perf_counter()
+        levels = self.pool.map(_cpu_worker, insts, chunksize=1)
+        return len(insts), time.perf_counter() - t0, levels
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def cpu_baseline(insts, name):
+    """The reference algorithm on the host cores: throughput with one instance
+    per process on every core, and the reference as shipped (one process:
+    single-threaded assembly, BLAS on all threads) on a short sample."""
+    pool = CpuPool()
+    n, dt, levels = pool.run([insts[q % len(insts)] for q in range(pool.n)])
+    pool.close()
+    n1, dt1, levels1 = cpu_sample(insts, 8.0)
+    return {"value": n / dt, "unit": "solves/s", "cores": pool.n, "kind": "port",
+            "sample": "first %d instances of the %s workload (levels %s), one per process on %d processes; "
+                      "oracle: C assembly and scipy LAPACK, one BLAS thread each" % (n, name, levels, pool.n),
+            "as_shipped": {"value": n1 / dt1, "unit": "solves/s",
+                           "sample": "first %d instance(s) in one process: single-threaded assembly as in the "
+                                     "reference, scipy LAPACK on all threads (levels %s)" % (n1, levels1)}}
+
+
 def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
     insts = workload(args.workload, args.instances)
-    cores = os.cpu_count()
-    # each step: one instance of the workload (cycling), the oracle on all cores
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
-    orc.lib()
+    pool = CpuPool()
+    cores = pool.n
+    # each step: one instance per process (cycling through the workload)
+    batch = lambda k: [insts[(k * cores + q) % len(insts)] for q in range(cores)]
     for k in range(max(args.warmup, 1)):  # untimed
-        cpu_solve(orc, insts[k % len(insts)])
+        pool.run(batch(k))
     t0 = time.perf_counter()
     n = 0
     for k in range(args.steps):
-        cpu_solve(orc, insts[k % len(insts)])
-        n += 1
+        n += pool.run(batch(args.warmup + k))[0]
     dt = time.perf_counter() - t0
+    pool.close()
     v = n / dt
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
@@ -243,9 +311,9 @@ def run_reference(args, rank, ws, dist):
             "config": config_of(args, insts, ws),
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": "%d instances of the %s workload, one per step (oracle: C assembly "
-                                       "single-threaded as in the reference, scipy LAPACK on %d threads)"
-                                       % (n, args.workload, cores)},
+                             "sample": "%d instances of the %s workload, %d per step, one per process on %d "
+                                       "processes (oracle: C assembly and scipy LAPACK, one BLAS thread each)"
+                                       % (n, args.workload, cores, cores)},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -429,10 +497,7 @@ def main():
                 "max_rel_err_mixed_vs_fp64": max(errs)}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        n, dt, levels = cpu_sample(insts, 20.0)
-        cpu = {"value": n / dt, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "first %d instance(s) of the %s workload (levels %s), oracle with C assembly on 1 thread "
-                         "and scipy LAPACK on all threads" % (n, args.workload, levels)}
+        cpu = cpu_baseline(insts, args.workload)
     if rank != 0:
         return
     line = {
