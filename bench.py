@@ -147,11 +147,6 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
-# FP64 rate of the GB300 (TFLOP/s): a DFMA / DMMA throughput probe measured
-# 0.99-1.05; MEASURED_PEAKS.json carries no FP64 figure.
-FP64_PEAK_TFLOPS = 1.0
-
-
 def traffic_of(cls, launches, flops):
     """DRAM bytes per launch of a kernel class from the committed ncu summary:
     'cls dram_bytes_per_flop X' (measured on a smaller capture, scaled by the
@@ -222,6 +217,14 @@ def cpu_sample(insts, budget_s=20.0):
 BLAS_THREAD_VARS = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
 
 
+def host_cores():
+    """CPUs this process may run on (affinity mask / cpuset), else all CPUs."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def _cpu_init():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
@@ -233,22 +236,35 @@ def _cpu_wait(seconds):
     return 0
 
 
-def _cpu_worker(inst):
-    """One instance through the oracle in a pool process."""
+def _cpu_worker(job):
+    """One instance through the oracle in a pool process: (index, level, seconds)."""
     import oracle as orc
+    k, inst = job
+    t0 = time.perf_counter()
     cpu_solve(orc, inst)
-    return inst["sphere_level"]
+    return k, inst["sphere_level"], time.perf_counter() - t0
+
+
+def mix_rate(per_level, insts, cores):
+    """Throughput of `cores` busy processes on the workload's level mix, from
+    the mean seconds per solve at each level."""
+    mean = {lev: sum(v) / len(v) for lev, v in per_level.items() if v}
+    lv = [i["sphere_level"] for i in insts if i["sphere_level"] in mean]
+    if not lv:
+        return None
+    return cores / (sum(mean[x] for x in lv) / len(lv))
 
 
 class CpuPool:
     """The reference algorithm's throughput on all host cores: one spawned
     process per core, whole instances each, BLAS on one thread per process
-    (independent solves, as the instances of a sweep are)."""
+    (independent solves, as the instances of a sweep are).  Instances stream
+    through the pool with no barrier between them, so every core stays busy."""
 
     def __init__(self):
         import multiprocessing as mp
         _cpu_init()  # builds the oracle here if needed, before the workers load it
-        self.n = os.cpu_count() or 1
+        self.n = host_cores()
         saved = {k: os.environ.get(k) for k in BLAS_THREAD_VARS}
         for k in BLAS_THREAD_VARS:
             os.environ[k] = "1"  # read by the children's BLAS at load time
@@ -262,10 +278,12 @@ class CpuPool:
                     os.environ[k] = v
         self.pool.map(_cpu_wait, [0.5] * self.n, chunksize=1)  # every worker up and loaded
 
-    def run(self, insts):
+    def stream(self, insts):
+        """Solve insts (in order, all cores busy); returns [(index, level,
+        seconds)] in completion order and the wall time."""
         t0 = time.perf_counter()
-        levels = self.pool.map(_cpu_worker, insts, chunksize=1)
-        return len(insts), time.perf_counter() - t0, levels
+        out = list(self.pool.imap_unordered(_cpu_worker, list(enumerate(insts)), chunksize=1))
+        return out, time.perf_counter() - t0
 
     def close(self):
         self.pool.close()
@@ -273,16 +291,24 @@ class CpuPool:
 
 
 def cpu_baseline(insts, name):
-    """The reference algorithm on the host cores: throughput with one instance
-    per process on every core, and the reference as shipped (one process:
+    """The reference algorithm on the host cores: throughput with every core
+    busy (two instances per core, streamed; each solve timed, projected to the
+    workload's level mix), and the reference as shipped (one process:
     single-threaded assembly, BLAS on all threads) on a short sample."""
     pool = CpuPool()
-    n, dt, levels = pool.run([insts[q % len(insts)] for q in range(pool.n)])
+    sample = [insts[q % len(insts)] for q in range(2 * pool.n)]
+    done, wall = pool.stream(sample)
     pool.close()
+    per_level = {}
+    for _, lev, sec in done:
+        per_level.setdefault(lev, []).append(sec)
     n1, dt1, levels1 = cpu_sample(insts, 8.0)
-    return {"value": n / dt, "unit": "solves/s", "cores": pool.n, "kind": "port",
-            "sample": "first %d instances of the %s workload (levels %s), one per process on %d processes; "
-                      "oracle: C assembly and scipy LAPACK, one BLAS thread each" % (n, name, levels, pool.n),
+    return {"value": mix_rate(per_level, insts, pool.n), "unit": "solves/s", "cores": pool.n, "kind": "port",
+            "sample": "first %d instances of the %s workload streamed through %d processes (all busy; oracle: C "
+                      "assembly and scipy LAPACK, one BLAS thread each); each solve timed, the mean seconds per "
+                      "sphere level projected to the workload's level mix" % (len(sample), name, pool.n),
+            "seconds_per_solve_by_level": {lev: sum(v) / len(v) for lev, v in per_level.items()},
+            "completed_over_wall": len(done) / wall,
             "as_shipped": {"value": n1 / dt1, "unit": "solves/s",
                            "sample": "first %d instance(s) in one process: single-threaded assembly as in the "
                                      "reference, scipy LAPACK on all threads (levels %s)" % (n1, levels1)}}
@@ -294,26 +320,31 @@ def run_reference(args, rank, ws, dist):
     insts = workload(args.workload, args.instances)
     pool = CpuPool()
     cores = pool.n
-    # each step: one instance per process (cycling through the workload)
-    batch = lambda k: [insts[(k * cores + q) % len(insts)] for q in range(cores)]
-    for k in range(max(args.warmup, 1)):  # untimed
-        pool.run(batch(k))
-    t0 = time.perf_counter()
-    n = 0
-    for k in range(args.steps):
-        n += pool.run(batch(args.warmup + k))[0]
-    dt = time.perf_counter() - t0
+    # a step is `cores` instances of the workload (in order, cycling); all steps
+    # stream through the pool without a barrier between them, the warm-up
+    # steps' solves first, and each solve is timed in its worker
+    nw = max(args.warmup, 1) * cores
+    seq = [insts[q % len(insts)] for q in range(nw + args.steps * cores)]
+    done, wall = pool.stream(seq)
     pool.close()
-    v = n / dt
+    per_level = {}
+    timed = [(k, lev, sec) for k, lev, sec in done if k >= nw]
+    for _, lev, sec in timed:
+        per_level.setdefault(lev, []).append(sec)
+    v = mix_rate(per_level, insts, cores)
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * cores / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_of(args, insts, ws),
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": "%d instances of the %s workload, %d per step, one per process on %d "
-                                       "processes (oracle: C assembly and scipy LAPACK, one BLAS thread each)"
-                                       % (n, args.workload, cores, cores)},
+                             "sample": "%d instances of the %s workload (%d per step) streamed through %d processes "
+                                       "with no barrier between them (oracle: C assembly and scipy LAPACK, one BLAS "
+                                       "thread each); each solve timed in its worker, the mean seconds per sphere "
+                                       "level projected to the workload's level mix"
+                                       % (len(timed), args.workload, cores, cores),
+                             "seconds_per_solve_by_level": {lev: sum(x) / len(x) for lev, x in per_level.items()},
+                             "completed_over_wall": len(done) / wall},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -402,6 +433,7 @@ def main():
     prec = sqbem.MIXED if args.precision == "mixed" else sqbem.FP64
     insts = workload(args.workload, args.instances, rank)
     peaks = load_peaks()
+    sqbem.set_limits(-1, -1)
     for _ in range(args.warmup):  # >= 3 for a valid bench line
         sqbem.kinematics_batch(insts, prec)
     sqbem.kernel_stats_enable(True)
@@ -424,32 +456,16 @@ def main():
     gpu_s = allmax(dist, gpu_s)
     wall = allmax(dist, wall)
     solves = allsum(dist, float(len(insts) * args.steps))
-    # dominant kernel class of the timed region
+    # kernel classes of the timed region (per-launch CUDA events; with six
+    # concurrent streams a launch's duration includes co-scheduled kernels)
     stats = {c: sqbem.kernel_stats(c) for c in sqbem.kernel_stats_classes()}
     sqbem.kernel_stats_enable(False)
-
-    def roofline_of(st, note):
-        top = max(st, key=lambda c: st[c][1]) if st else None
-        if not top:
-            return None
-        nl, secs, fl, by = st[top]
-        if top in ("tc_gemm",):
-            achieved, peak, unit, bound = fl / secs / 1e12, peaks["bf16_tflops"], "TFLOP/s", "tensor"
-        elif top == "dgemm":
-            achieved, peak, unit, bound = fl / secs / 1e12, FP64_PEAK_TFLOPS, "TFLOP/s (fp64)", "tensor"
-        else:
-            achieved, peak, unit, bound = by / secs / 1e9, peaks["hbm_gbs"], "GB/s", "hbm"
-        return {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
-                "launch_seconds": secs, "peak_source": peaks["source"] if top != "dgemm" else "fp64 probe",
-                "note": note}
-
-    roofline = roofline_of(stats, "per-launch CUDA events over the timed region; with concurrent streams a "
-                                  "launch's duration includes the kernels of other streams sharing the GPU")
-    # the same classes from one extra, untimed step on a single stream: the
-    # kernels' own rates, without co-scheduling
-    roofline_1s, st1 = None, None
-    if rank == 0 and args.impl == "gb300":
+    step_s = gpu_s / args.steps
+    # the kernels' own rates: the same workload once more, untimed, on a single
+    # stream, every launch bracketed by CUDA events on its stream
+    st1, fp64_peak, fp32_peak = None, None, None
+    if rank == 0:
+        fp64_peak, fp32_peak = sqbem.pipe_rates()
         prev = os.environ.get("SQBEM_STREAMS")
         os.environ["SQBEM_STREAMS"] = "1"
         sqbem.kernel_stats_enable(True)
@@ -460,41 +476,85 @@ def main():
             del os.environ["SQBEM_STREAMS"]
         else:
             os.environ["SQBEM_STREAMS"] = prev
-        roofline_1s = roofline_of(st1, "one untimed step on a single stream, per-launch CUDA events")
+
+    def roofline_of(st):
+        top = max(st, key=lambda c: st[c][1]) if st else None
+        if not top:
+            return None
+        nl, secs, fl, by = st[top]
+        if top == "tc_gemm":
+            achieved, peak, unit, bound, src = fl / secs / 1e12, peaks["bf16_tflops"], "TFLOP/s", "tensor", \
+                peaks["source"]
+        elif top in ("dgemm", "assemble_near"):
+            achieved, peak, unit, bound, src = fl / secs / 1e12, fp64_peak, "TFLOP/s (fp64)", "fp64", \
+                "measured now (sqbem_pipe_rates)"
+        else:
+            achieved, peak, unit, bound, src = by / secs / 1e9, peaks["hbm_gbs"], "GB/s", "hbm", peaks["source"]
+        # one step's worth of this class cannot take longer than the step
+        assert secs <= step_s * 1.0001 or args.workload != "sweep" or ws > 1, \
+            "%s: %.3f s of kernel time in one single-stream step > %.3f s per step" % (top, secs, step_s)
+        return {"kernel": top, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak, "traffic": traffic_of(top, nl, fl), "launches": nl,
+                "launch_seconds": secs, "share_of_step": secs / step_s, "peak_source": src,
+                "note": "one untimed step of the same workload on a single stream right after the timed region; "
+                        "per-launch CUDA events on the launching stream; achieved = credited work / summed "
+                        "launch durations"}
+
+    roofline = roofline_of(st1) if st1 else None
     # assembly throughput: far-kernel flops are credited at 7 x FLOPS_PER_EVAL (= 64,
-    # csrc/assemble.cuh) per (target, panel) pair
+    # csrc/assemble.cuh) per (target, panel) pair; near-kernel flops per rule
+    # from the pair counts (FP64 work: 448-point rule and self integral in mixed mode)
     assembly = None
-    kst = st1 if roofline_1s is not None else stats  # kernel durations without co-scheduling
-    if "assemble_far" in kst:
-        _, s_far, f_far, b_far = kst["assemble_far"]
-        s_near = kst.get("assemble_near", (0, 0.0, 0.0, 0.0))[1]
+    if st1 and "assemble_far" in st1:
+        _, s_far, f_far, b_far = st1["assemble_far"]
+        _, s_near, f_near, _ = st1.get("assemble_near", (0, 0.0, 0.0, 0.0))
         pairs = f_far / (7 * 64)
-        steps_in = 1 if roofline_1s is not None else args.steps
-        assembly = {"panel_pairs_per_step": pairs / steps_in, "pairs_per_s": pairs / (s_far + s_near),
+        mixed = prec == sqbem.MIXED
+        assembly = {"panel_pairs_per_step": pairs, "pairs_per_s": pairs / (s_far + s_near),
                     "far_kernel_written_gbs": b_far / s_far / 1e9,
                     "far_kernel_frac_of_hbm": b_far / s_far / 1e9 / peaks["hbm_gbs"],
-                    "seconds_far_near": [s_far, s_near]}
-    # plain FP64 GPU path on the same workload: per-level samples, projected to
-    # the workload's level mix; the mixed results are checked against it
+                    "far_kernel_tflops": f_far / s_far / 1e12,
+                    "far_kernel_frac_of_pipe": f_far / s_far / 1e12 / (fp32_peak if mixed else fp64_peak),
+                    "far_pipe": "fp32" if mixed else "fp64",
+                    "near_kernel_fp64_tflops": f_near / s_near / 1e12 if s_near else None,
+                    "near_kernel_frac_of_fp64": f_near / s_near / 1e12 / fp64_peak if s_near else None,
+                    "seconds_far_near": [s_far, s_near],
+                    "pipe_peaks_tflops": {"fp64": fp64_peak, "fp32": fp32_peak,
+                                          "source": "measured now (sqbem_pipe_rates: FMA chains on every SM)"}}
+    # plain FP64 GPU path on the whole workload: its rate, and every mixed
+    # result compared with it (U, Omega per slip mode; sphere and wall tractions)
     fp64 = None
     if rank == 0 and prec == sqbem.MIXED and not args.no_fp64 and args.workload == "sweep":
         import numpy as np
-        per_level, errs = {}, []
-        for lev in sorted({i["sphere_level"] for i in insts}):
-            idx = [k for k, i in enumerate(insts) if i["sphere_level"] == lev][:6]
-            sample = [insts[k] for k in idx]
-            sqbem.kinematics_batch(sample[:1], sqbem.FP64)
-            r64, s64 = sqbem.kinematics_batch(sample, sqbem.FP64)
-            per_level[lev] = s64 / len(sample)
-            for j, k in enumerate(idx):
-                a, b = results[k][:12], r64[j][:12]
-                errs.append(float(np.max(np.abs(a - b)) / np.max(np.abs(b))))
-        t64 = sum(per_level[i["sphere_level"]] for i in insts)
-        fp64 = {"value": len(insts) / t64, "unit": "solves/s",
-                "sample": "6 instances per sphere level of the same workload, FP64 GPU path, projected to its "
-                          "level mix", "seconds_per_solve_by_level": per_level,
-                "mixed_over_fp64": (solves / gpu_s) / (len(insts) / t64) if ws == 1 else None,
-                "max_rel_err_mixed_vs_fp64": max(errs)}
+        rm, _, fsm, ftm = sqbem.kinematics_batch(insts, sqbem.MIXED, tractions=True)
+        sqbem.kinematics_batch(insts[:1], sqbem.FP64)
+        r64, s64, fs64, ft64 = sqbem.kinematics_batch(insts, sqbem.FP64, tractions=True)
+        # each instance is a squirmer with B2/B1 = alpha (the workload's draw):
+        # U = U_B1 + alpha U_B2 and likewise Omega and the tractions
+        errs = {"U": [], "Omega": [], "U_Omega_both_modes": [], "f_sphere": [], "f_tube": []}
+        for k, inst in enumerate(insts):
+            al = inst.get("alpha", 0.0)
+            comb = lambda r, j: r[k][j:j + 3] + al * r[k][6 + j:9 + j]
+            U, U64, W, W64 = comb(rm, 0), comb(r64, 0), comb(rm, 3), comb(r64, 3)
+            errs["U"].append(float(np.linalg.norm(U - U64) / np.linalg.norm(U64)))
+            # rotation rates in units of U/a (a = 1): Omega -> 0 on the axis
+            errs["Omega"].append(float(np.linalg.norm(W - W64) / max(np.linalg.norm(W64), np.linalg.norm(U64))))
+            errs["U_Omega_both_modes"].append(float(np.linalg.norm(rm[k][:12] - r64[k][:12]) /
+                                                    np.linalg.norm(r64[k][:12])))
+            for q, A, B in (("f_sphere", fsm[k], fs64[k]), ("f_tube", ftm[k], ft64[k])):
+                if B.size:
+                    fa, fb = A[0] + al * A[1], B[0] + al * B[1]
+                    errs[q].append(float(np.max(np.abs(fa - fb)) / np.max(np.abs(fb))))
+        per_q = {q: {"max": max(v), "median": float(np.median(v)), "count": len(v)} for q, v in errs.items() if v}
+        fp64 = {"value": len(insts) / s64, "unit": "solves/s",
+                "sample": "the whole workload through the FP64 GPU path (same batching)",
+                "mixed_over_fp64": (solves / gpu_s) / (len(insts) / s64) if ws == 1 else None,
+                "instances_compared": len(insts),
+                "max_rel_err_mixed_vs_fp64": max(per_q["U"]["max"], per_q["Omega"]["max"]),
+                "rel_err_mixed_vs_fp64": per_q,
+                "error_norms": "per instance, for its squirmer B2/B1 = alpha: U |dU|/|U|; Omega "
+                               "|dOmega|/max(|Omega|, |U|/a); U_Omega_both_modes |d(U,Omega)_B1,B2|/|(U,Omega)_B1,B2|; "
+                               "f_sphere, f_tube max|df|/max|f| of f_B1 + alpha f_B2"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(insts, args.workload)
@@ -511,7 +571,6 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
-        "roofline_single_stream": roofline_1s,
         "assembly": assembly,
         "fp64_gpu": fp64,
         "cpu_baseline": cpu,

@@ -17,6 +17,9 @@
  *     on distinct handles may run on different host threads.
  *   - There is no CPU fallback: without a CUDA device, compute entry points
  *     return SQBEM_ERR_NO_DEVICE.
+ *   - Device state the library sets up once per process (quadrature tables,
+ *     kernel attributes, cached device addresses) does not survive a
+ *     cudaDeviceReset by the caller: do not call the library after one.
  */
 #ifndef SQBEM_H
 #define SQBEM_H
@@ -50,6 +53,28 @@ const char* sqbem_last_error(void);
 const char* sqbem_version(void);
 /* Number of kernel launches issued by this process so far (all entry points). */
 long long sqbem_launch_count(void);
+/* Limits of the device-side safeguards (no counterpart in the reference, whose
+ * LAPACK calls neither wait on the device nor iterate):
+ *   gemm_wait_cycles       SM clock cycles a role of the tensor-core GEMM waits
+ *                          for one pipeline stage before the call fails with
+ *                          SQBEM_ERR_TIMEOUT (default 4e9, about 2 s);
+ *   refine_max_iterations  mixed-precision refinement steps before the call
+ *                          fails with SQBEM_ERR_NOT_CONVERGED (default 30; 0
+ *                          allows none, so every mixed solve then fails).
+ * A negative value restores the default.  Process-wide; affects calls that
+ * start after it returns. */
+int sqbem_set_limits(long long gemm_wait_cycles, int refine_max_iterations);
+/* Test hook for the timeout path (no counterpart in the reference): the next
+ * `calls` calls of the tensor-core GEMM each make one of their waits a wait on
+ * a barrier that nothing completes, so it runs out after gemm_wait_cycles and
+ * the entry point that issued the GEMM returns SQBEM_ERR_TIMEOUT, with the
+ * device and the library usable afterwards.  0 cancels pending stalls. */
+int sqbem_test_gemm_stall(int calls);
+/* FMA throughput of this GPU's FP64 and FP32 pipes in TFLOP/s (2 flops per
+ * FMA), measured on the spot with independent FMA chains on every SM (about
+ * 40 ms; no counterpart in the reference).  The benchmark divides the
+ * assembly kernels' flop rates by these. */
+int sqbem_pipe_rates(double* fp64_tflops, double* fp32_tflops);
 /* Host->device and device->host bytes copied by the library so far. */
 int sqbem_transfer_bytes(long long* h2d, long long* d2h);
 /* Opt-in per-kernel-class timing (no counterpart in the reference; used by the
@@ -111,6 +136,24 @@ int sqbem_solve_dense(int n, int nrhs, const double* A, double* B, int* pivoted)
  * Relative accuracy about 2^-16 per product. */
 int sqbem_gemm_mixed(int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
                      float beta, float* C, int ldc);
+/* The same with the kernel's tile variant chosen by the caller (-1: the one
+ * the tuning table gives for the shape; see sqbem_gemm_variants) and 3
+ * products (hi*hi + hi*lo + lo*hi) or 2 (hi*hi + hi*lo: A rounded to BF16,
+ * about 2^-8 relative per product).  No counterpart in the reference. */
+int sqbem_gemm_mixed_ex(int variant, int products, int M, int N, int K, float alpha, const float* A, int lda,
+                        const float* B, int ldb, float beta, float* C, int ldc);
+/* Number of tile variants of the tensor-core GEMM kernel (0: 128 x 128 tiles,
+ * 3-stage pipeline; 1: 128 x 256 tiles, 2 stages).  The library picks one per
+ * launch from the tuning table tuning/tc_gemm.txt beside lib/ (written by the
+ * package's tune_gemm.py; SQBEM_TC_TABLE names another file, SQBEM_TC_VARIANT
+ * forces one variant).  No counterpart in the reference. */
+int sqbem_gemm_variants(int* count);
+/* Device time of one grouped launch of `count` (<= 48) problems M x N x K with
+ * device-resident pseudo-random split operands, averaged over `reps` launches
+ * after one warm-up (the tuner's and the profiles' measurement; no host copies
+ * in the timed region).  No counterpart in the reference. */
+int sqbem_gemm_timing(int variant, int products, int M, int N, int K, int count, float beta, int reps,
+                      double* seconds);
 
 /* ---------------------------------------------------------------- field
  * velocity_at, src/utils/field.hpp:18-34: lab-frame velocity at npts points
@@ -128,10 +171,12 @@ int sqbem_velocity_at(int P, const double* V, const double* u, const double* f, 
  * need live in a file-scope device array for at most
  * SQBEM_NOALLOC_MAX_PANELS panels (2.3 MB, held by every GPU that loads the
  * library until the process exits); larger P is rejected with SQBEM_ERR_ARG.
- * The array's device address is looked up on the first call on each device,
- * so make that first call before any stream capture.  Every call shares the
- * array and overwrites it: calls that overlap on the GPU race.  The call
- * returns after its work on `stream` has completed. */
+ * The first call on each device does a one-time set-up: it looks up the
+ * array's device address (cached per device ordinal) and uploads the library's
+ * quadrature tables, which synchronizes the whole device; make that first call
+ * before any stream capture begins.  Every call shares the array and
+ * overwrites it: calls that overlap on the GPU race.  The call returns after
+ * its work on `stream` has completed. */
 #define SQBEM_NOALLOC_MAX_PANELS 16384
 int sqbem_velocity_at_noalloc(int P, const double* V, const double* u, const double* f, double mu, int npts,
                               const double* pts, double* out, int precision, void* stream);
@@ -218,6 +263,13 @@ typedef struct {
 #define SQBEM_RESULT_STRIDE 16
 int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
                            double* device_seconds);
+/* The same batch, also returning the tractions of the solves (the f_sphere
+ * and f_tube of SwimmerSolution, swimmer.hpp:78-81): for instance k,
+ * f_sphere[k] receives 2 x 3 Ns values (the B1 = 1 mode, then the B2 = 1
+ * mode; Ns = 20 * 4^sphere_level) and f_tube[k] 2 x 3 Nt values (Nt as in
+ * results).  Either array, or any entry of it, may be NULL. */
+int sqbem_kinematics_batch_tractions(int n, const sqbem_instance* inst, int precision, double* results,
+                                     double* const* f_sphere, double* const* f_tube, double* device_seconds);
 
 /* Batched adjoint sensitivities: instance k as in sqbem_kinematics_batch
  * (towed ignored), FP64 only.  results[k * SQBEM_ADJOINT_STRIDE + 24 m + ...]
@@ -247,6 +299,18 @@ typedef struct {
 } sqbem_traj_params;
 
 int sqbem_trajectory_defaults(sqbem_traj_params* p);
+
+/* Factored tubes shared across calls (the tube factor cache of the
+ * trajectory calls; the reference factors its tube once per run_trajectory,
+ * src/trajectory.hpp:47).  sqbem_run_trajectory, sqbem_trajectory_ensemble and
+ * sqbem_ensemble_field take their tube -- keyed by R, L, a, n_theta, n_r, mu
+ * and the precision mode -- from a process-wide least-recently-used cache of
+ * SQBEM_TUBE_CACHE entries (environment variable, default 4, 0 = off), so
+ * calls with the same tube assemble and factor it once.  stats: tubes built
+ * and cache hits so far, entries held; clear drops every entry (memory is
+ * returned once no running call uses it). */
+int sqbem_tube_cache_stats(long long* builds, long long* hits, int* entries);
+int sqbem_tube_cache_clear(void);
 
 /* run_trajectory, src/trajectory.hpp:42-151: integrates (or resumes) one
  * trajectory -- 3 RK4 start-up steps then 4th-order Adams-Bashforth, |e|

@@ -3,8 +3,9 @@
     python squirmer-bem-3dtube_gb300/build.py [--force]
 
 Compiles every csrc/*.cu in parallel with nvcc (one -gencode, sm_103a) and links
-them into lib/libsqbem.so.  Objects go to _build/ (git-ignored); a source is
-recompiled only when it or a header changed.
+them into lib/libsqbem.so, then the command-line program cli/squirmer_bem.cpp
+(host C++ over the drop-in headers) into bin/squirmer_bem.  Objects go to
+_build/ (git-ignored); a source is recompiled only when it or a header changed.
 """
 import glob
 import os
@@ -17,6 +18,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "lib", "libsqbem.so")
+CLI_SRC = os.path.join(PKG, "cli", "squirmer_bem.cpp")
+CLI = os.path.join(PKG, "bin", "squirmer_bem")
+CXX = os.environ.get("CXX", "g++")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -64,6 +68,14 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    if force or _stale(CLI, [CLI_SRC, LIB] + hdrs):
+        cmd = [CXX, "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+               "-I" + os.path.join(PKG, "include", "bem"), CLI_SRC, "-L" + os.path.dirname(LIB), "-lsqbem",
+               "-Wl,-rpath,$ORIGIN/../lib", "-o", CLI]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("building the command-line program failed:\n%s%s" % (r.stdout, r.stderr))
     return LIB
 
 

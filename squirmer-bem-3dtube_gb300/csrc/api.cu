@@ -34,6 +34,11 @@ void require_device() {
 
 void set_last_error(const char* msg) { g_last_error = msg; }
 
+static std::atomic<long long> g_wait_cycles{DEFAULT_WAIT_CYCLES};
+static std::atomic<int> g_refine_max_it{DEFAULT_REFINE_MAX_IT};
+long long gemm_wait_cycles() { return g_wait_cycles.load(std::memory_order_relaxed); }
+int refine_max_iterations() { return g_refine_max_it.load(std::memory_order_relaxed); }
+
 // Per-panel geometry exactly as Mesh::geometry (mesh.hpp:61-72).
 std::vector<PanelRec> make_panels(const double* V, int P) {
     std::vector<PanelRec> out((size_t)P);
@@ -155,6 +160,14 @@ using namespace sqbem;
 extern "C" const char* sqbem_last_error(void) { return g_last_error.c_str(); }
 extern "C" const char* sqbem_version(void) { return "sqbem 0.1 (sm_103a)"; }
 extern "C" long long sqbem_launch_count(void) { return g_launches.load(); }
+
+extern "C" int sqbem_set_limits(long long gemm_wait_cycles, int refine_max_iterations) {
+    return guarded([&] {
+        if (refine_max_iterations > 1000) fail(SQBEM_ERR_ARG, "set_limits: at most 1000 refinement steps");
+        g_wait_cycles.store(gemm_wait_cycles < 0 ? DEFAULT_WAIT_CYCLES : gemm_wait_cycles);
+        g_refine_max_it.store(refine_max_iterations < 0 ? DEFAULT_REFINE_MAX_IT : refine_max_iterations);
+    });
+}
 
 // ---------------------------------------------------------------- geometry
 static int put_mesh(const bem::Mesh& m, double* V, int* tags, int cap, int* P) {

@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
         const int rule = (job.same_mesh && p == i) ? 4 : rule_of(P, x, y, z);
         if (rule != 0) {
             near_append(job, i, p, rule);
+            if (job.rule_count) atomicAdd(job.rule_count + rule, 1);
             continue;
         }
         Acc<double> A;
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
                                                           const float* __restrict__ tgtf) {
     __shared__ FarF sf[FAR_SRC];
     __shared__ int2 nl[FAR_PAIRS];
-    __shared__ int ncount[2], nbase[2];
+    __shared__ int ncount[2], nbase[2], rcount[5];
     const int p0 = blockIdx.y * FAR_SRC;
     const int ns = min(FAR_SRC, job.nS - p0);
     {
@@ -411,6 +412,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         for (int k = threadIdx.x; k < n4; k += blockDim.x) d4[k] = s4[k];
     }
     if (threadIdx.x < 2) ncount[threadIdx.x] = 0;
+    if (threadIdx.x < 5) rcount[threadIdx.x] = 0;
     __syncthreads();
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     const int nsi = i < job.nT ? ns : 0;  // targets past the end take part in the barriers only
@@ -438,6 +440,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
             const bool heavy = rule >= 3;
             const int slot = atomicAdd(&ncount[heavy ? 0 : 1], 1);  // at most FAR_PAIRS in total
             nl[heavy ? slot : FAR_PAIRS - 1 - slot] = make_int2(i, p | (rule << 28));
+            if (job.rule_count) atomicAdd(&rcount[rule], 1);
             continue;
         }
         Acc<float> A;
@@ -465,6 +468,8 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         const int n = ncount[threadIdx.x];
         nbase[threadIdx.x] = n > 0 ? atomicAdd(job.near_count + threadIdx.x, n) : 0;
     }
+    if (job.rule_count && threadIdx.x >= 1 && threadIdx.x < 5 && rcount[threadIdx.x] > 0)
+        atomicAdd(job.rule_count + threadIdx.x, rcount[threadIdx.x]);
     __syncthreads();
     const int nh = ncount[0], nlt = ncount[1], cap = job.near_cap;
     for (int e = threadIdx.x; e < nh; e += FAR_TGT) {
@@ -532,6 +537,12 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
     job.near_list = list.get();
     job.near_count = count.get();
     job.near_cap = near_cap;
+    DevBuf<int> rc;
+    if (kstats_on()) {
+        rc.alloc(5, st);
+        rc.zero();
+        job.rule_count = rc.get();
+    }
     dim3 grid(ceil_div(job.nT, FAR_TGT), ceil_div(job.nS, FAR_SRC));
     // credited work: every pair considered, at the 7-point rule; bytes written
     const double pairs = (double)job.nT * job.nS;
@@ -554,13 +565,26 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
         CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     });
     const int warps = sms * 24;  // 3 CTAs of 8 warps per SM (80 registers per thread)
+    // credited FP64-pipe work of the near kernel (kernel statistics only, which
+    // count the pairs per rule on the device): the 448-point rule and the self
+    // integral, plus in FP64 mode the 28- and 112-point rules (FP32 in mixed mode)
     if (kstats_on()) {
+        int* counts = kstat_pinned_ints(5);
+        CUDA_CHECK(cudaMemcpyAsync(counts, rc.get(), 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        const double w[5] = {0.0, mixed ? 0.0 : 28.0 * FLOPS_PER_EVAL, mixed ? 0.0 : 112.0 * FLOPS_PER_EVAL,
+                             448.0 * FLOPS_PER_EVAL, 300.0 * FLOPS_PER_EVAL_SL};
         char note[96];
         std::snprintf(note, sizeof note, "nT=%d nS=%d same=%d mixed=%d", job.nT, job.nS, job.same_mesh, (int)mixed);
         kstat_note(note);
+        const int ks = kstat_begin(st);
+        if (mixed) LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
+        else LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
+        kstat_end_counted(ks, "assemble_near", st, counts, w, 5, 0.0);
+    } else if (mixed) {
+        LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
+    } else {
+        LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
     }
-    if (mixed) TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
-    else TIMED_LAUNCH("assemble_near", 0.0, 0.0, (near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
     if ((long long)job.nT * job.nS > near_cap) {
         // the list could overflow only for blocks larger than its capacity
         int h[3] = {};

@@ -11,6 +11,8 @@ namespace sqbem {
 // FMA = 2): r from the vertex vectors 15, |r|^2 5, 1/|r| 1, powers 2, s 1,
 // r.m 5, d 3, diagonal 2, s r 3, SL 12, d r 3, DL 12.
 constexpr double FLOPS_PER_EVAL = 64.0;
+// The self integral's evaluations form SL only: without r.m 5, d 3, d r 3, DL 12.
+constexpr double FLOPS_PER_EVAL_SL = 41.0;
 
 struct PanelRec {
     double v[9];
@@ -38,6 +40,7 @@ struct BlockJob {
     int2* near_list = nullptr;
     int* near_count = nullptr;  // [heavy, light, work counter] (assemble.cu)
     int near_cap = 0;
+    int* rule_count = nullptr;  // [5]: near pairs per rule, counted only for kernel statistics
 };
 
 struct FieldJob {

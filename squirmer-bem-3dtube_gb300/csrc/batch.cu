@@ -41,6 +41,52 @@ std::vector<double> squirmer_slip_host(const std::vector<PanelRec>& S, const dou
     return u;
 }
 
+namespace sqbem {
+namespace {
+constexpr int SLIP_MAXJ = 64;
+struct SlipArgs {
+    int n;
+    SlipJob j[SLIP_MAXJ];
+};
+
+// One panel per thread; the operations of squirmer_slip_host in its order,
+// rounded the same way (no contraction), so the two agree bit for bit.
+__global__ void slip_modes_kernel(const __grid_constant__ SlipArgs args) {
+    const SlipJob& J = args.j[blockIdx.y];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= J.Ns) return;
+    const PanelRec& P = J.rec[p];
+    const double rx = __dsub_rn(P.c[0], J.xc[0]), ry = __dsub_rn(P.c[1], J.xc[1]), rz = __dsub_rn(P.c[2], J.xc[2]);
+    const double nn = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+    const double inv = __ddiv_rn(1.0, __dsqrt_rn(nn));
+    const double hx = __dmul_rn(inv, rx), hy = __dmul_rn(inv, ry), hz = __dmul_rn(inv, rz);
+    const double ct = __dadd_rn(__dadd_rn(__dmul_rn(hx, J.e[0]), __dmul_rn(hy, J.e[1])), __dmul_rn(hz, J.e[2]));
+    const double vx = __dsub_rn(__dmul_rn(ct, hx), J.e[0]);
+    const double vy = __dsub_rn(__dmul_rn(ct, hy), J.e[1]);
+    const double vz = __dsub_rn(__dmul_rn(ct, hz), J.e[2]);
+    const double s1 = __dadd_rn(1.0, __dmul_rn(0.0, ct));  // B1 = 1, B2 = 0
+    const double s2 = __dadd_rn(0.0, __dmul_rn(1.0, ct));  // B1 = 0, B2 = 1
+    double* o1 = J.out + 3 * (long long)p;
+    double* o2 = J.out + 3 * ((long long)J.Ns + p);
+    o1[0] = __dmul_rn(s1, vx); o1[1] = __dmul_rn(s1, vy); o1[2] = __dmul_rn(s1, vz);
+    o2[0] = __dmul_rn(s2, vx); o2[1] = __dmul_rn(s2, vy); o2[2] = __dmul_rn(s2, vz);
+}
+}  // namespace
+
+void slip_modes_group(const std::vector<SlipJob>& jobs, cudaStream_t st) {
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += SLIP_MAXJ) {
+        SlipArgs a;
+        a.n = (int)std::min<size_t>(SLIP_MAXJ, jobs.size() - i0);
+        int mx = 0;
+        for (int k = 0; k < a.n; ++k) {
+            a.j[k] = jobs[i0 + k];
+            mx = std::max(mx, a.j[k].Ns);
+        }
+        if (mx > 0) LAUNCH(slip_modes_kernel, dim3((unsigned)ceil_div(mx, 128), (unsigned)a.n), 128, 0, st, a);
+    }
+}
+}  // namespace sqbem
+
 namespace {
 
 struct Prepared {
@@ -90,6 +136,16 @@ std::vector<Prepared> prepare_all(int n, const sqbem_instance* inst) {
     return prep;
 }
 
+// Where the results of a batch go: the fixed-stride records and, optionally,
+// the tractions of both slip modes per instance (host arrays, may be null).
+struct Outputs {
+    double* results = nullptr;
+    double* const* f_sphere = nullptr;  // [k]: 2 x 3 Ns (mode B1 = 1, then B2 = 1)
+    double* const* f_tube = nullptr;    // [k]: 2 x 3 Nt
+    double* fs(int k) const { return f_sphere ? f_sphere[k] : nullptr; }
+    double* ft(int k) const { return f_tube ? f_tube[k] : nullptr; }
+};
+
 void validate(const sqbem_instance& in) {
     if (!(in.a_over_R >= 0 && in.a_over_R < 1) || !(in.beta >= 0 && in.beta < 1) || !(in.L_over_R > 0) ||
         in.sphere_level < 0 || in.sphere_level > 5 || (in.a_over_R > 0 && (in.n_theta < 3 || in.n_r < 1)))
@@ -99,7 +155,8 @@ void validate(const sqbem_instance& in) {
 }
 
 // One instance through the same handles the single-instance API uses.
-void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStream_t bs, double* res) {
+void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStream_t bs, double* res,
+             double* f_sphere, double* f_tube) {
     std::unique_ptr<sqbem_tube> t;
     if (P.bounded) {
         t = std::make_unique<sqbem_tube>();
@@ -118,7 +175,7 @@ void run_one(const sqbem_instance& in, const Prepared& P, int precision, cudaStr
     std::vector<double> slips(u1);
     slips.insert(slips.end(), u2.begin(), u2.end());
     double U[6], Om[6];
-    s.solve_free(2, slips.data(), U, Om, nullptr, nullptr);
+    s.solve_free(2, slips.data(), U, Om, f_sphere, P.bounded ? f_tube : nullptr);
     for (int k = 0; k < 3; ++k) {
         res[k] = U[k];
         res[3 + k] = Om[k];
@@ -167,7 +224,8 @@ struct PhaseClock {
 // One chunk of a group (members with equal padded tube size and sphere size),
 // everything on stream bs.
 void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_instance* inst,
-               const std::vector<Prepared>& prep, cudaStream_t bs, double* results, PhaseClock& pc) {
+               const std::vector<Prepared>& prep, cudaStream_t bs, const Outputs& out, PhaseClock& pc) {
+    double* const results = out.results;
     const size_t G = ids.size();
     DevBuf<int> flags(2, bs);
     flags.zero();
@@ -203,22 +261,26 @@ void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_ins
     }
     mixed_build_swimmers(sp, cx);
     pc.lap("swimmers", G, ntp_k, ns_k);
-    // the B1 = 1 and B2 = 1 slip modes of every member
+    // the B1 = 1 and B2 = 1 slip modes of every member, on the device
     std::vector<DevBuf<double>> slip(G), xs(G);
     std::vector<const double*> in_ptr;
     std::vector<double*> x_ptr;
+    std::vector<SlipJob> sj;
     for (size_t g = 0; g < G; ++g) {
         sqbem_swimmer& s = *sws[g];
-        const double c[3] = {prep[ids[g]].b, 0, 0};
-        auto u1 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 1, 0);
-        const auto u2 = squirmer_slip_host(s.host_panels, c, inst[ids[g]].e, 0, 1);
-        u1.insert(u1.end(), u2.begin(), u2.end());
-        slip[g].alloc(u1.size(), bs);
-        slip[g].upload(u1.data(), u1.size());
+        slip[g].alloc((size_t)6 * s.Ns, bs);
+        SlipJob j;
+        j.rec = s.panels.rec.get();
+        j.Ns = s.Ns;
+        j.xc[0] = prep[ids[g]].b;
+        for (int q = 0; q < 3; ++q) j.e[q] = inst[ids[g]].e[q];
+        j.out = slip[g].get();
+        sj.push_back(j);
         xs[g].alloc((size_t)(s.mx.nt + s.mx.nc) * 2, bs);
         in_ptr.push_back(slip[g].get());
         x_ptr.push_back(xs[g].get());
     }
+    slip_modes_group(sj, bs);
     int iters = 0;
     double resid = 0;
     mixed_solve(sp, false, in_ptr, 2, x_ptr, cx, &iters, &resid);
@@ -272,6 +334,13 @@ void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_ins
         res[13] = s.Nt;
         res[14] = s.Ns;
         res[15] = iters;
+        // x = [f_t; f_s; w] per mode
+        for (int m = 0; m < 2; ++m) {
+            if (double* fs = out.fs(ids[g]))
+                std::memcpy(fs + (size_t)m * ns, hx[g].data() + (size_t)m * ldx + nt, sizeof(double) * ns);
+            if (double* ft = out.ft(ids[g]); ft && nt)
+                std::memcpy(ft + (size_t)m * nt, hx[g].data() + (size_t)m * ldx, sizeof(double) * nt);
+        }
     }
     for (size_t t = 0; t < towed.size(); ++t) {
         sqbem_swimmer& s = *towed[t];
@@ -290,7 +359,7 @@ double chunk_bytes(size_t G, int ntp, int ns) {
 }
 
 void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
-               double* results) {
+               const Outputs& out) {
     std::map<std::tuple<int, int, int>, std::vector<int>> groups;
     for (int k = 0; k < n; ++k) {
         const int ntp = prep[k].bounded ? pad128(3 * prep[k].tube.P()) : 0;
@@ -316,13 +385,13 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
     for (const Chunk& c : chunks) bytes.push_back(chunk_bytes(c.ids.size(), c.ntp, c.ns));
     run_concurrent(chunks.size(), bytes, bs, [&](size_t k, cudaStream_t st) {
         PhaseClock pc;
-        run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, results, pc);
+        run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, out, pc);
     });
 }
 
 // FP64: one instance per task, the same concurrency as the mixed path.
 void run_fp64(int n, const sqbem_instance* inst, const std::vector<Prepared>& prep, cudaStream_t bs,
-              double* results) {
+              const Outputs& out) {
     std::vector<int> order(n);
     for (int k = 0; k < n; ++k) order[k] = k;
     std::stable_sort(order.begin(), order.end(),
@@ -334,30 +403,50 @@ void run_fp64(int n, const sqbem_instance* inst, const std::vector<Prepared>& pr
     }
     run_concurrent((size_t)n, bytes, bs, [&](size_t j, cudaStream_t st) {
         const int k = order[j];
-        run_one(inst[k], prep[k], SQBEM_FP64, st, results + (size_t)k * SQBEM_RESULT_STRIDE);
+        run_one(inst[k], prep[k], SQBEM_FP64, st, out.results + (size_t)k * SQBEM_RESULT_STRIDE, out.fs(k), out.ft(k));
     });
 }
 
 }  // namespace
 
+namespace {
+void kinematics_batch(int n, const sqbem_instance* inst, int precision, const Outputs& out, double* device_seconds) {
+    if (n < 0 || (n > 0 && (!inst || !out.results)) || (precision != SQBEM_FP64 && precision != SQBEM_MIXED))
+        fail(SQBEM_ERR_ARG, "kinematics_batch: bad arguments");
+    for (int k = 0; k < n; ++k) validate(inst[k]);
+    if (device_seconds) *device_seconds = 0;
+    if (n == 0) return;
+    require_device();
+    const std::vector<Prepared> prep = prepare_all(n, inst);
+    Stream bs;
+    EventTimer clk;
+    clk.start(bs);
+    if (precision == SQBEM_MIXED) run_mixed(n, inst, prep, bs, out);
+    else run_fp64(n, inst, prep, bs, out);
+    clk.stop(bs);
+    const double secs = clk.seconds();
+    if (device_seconds) *device_seconds = secs;
+}
+}  // namespace
+
 extern "C" int sqbem_kinematics_batch(int n, const sqbem_instance* inst, int precision, double* results,
                                       double* device_seconds) {
     return guarded([&] {
-        if (n < 0 || (n > 0 && (!inst || !results)) || (precision != SQBEM_FP64 && precision != SQBEM_MIXED))
-            fail(SQBEM_ERR_ARG, "kinematics_batch: bad arguments");
-        for (int k = 0; k < n; ++k) validate(inst[k]);
-        if (device_seconds) *device_seconds = 0;
-        if (n == 0) return;
-        require_device();
-        const std::vector<Prepared> prep = prepare_all(n, inst);
-        Stream bs;
-        EventTimer clk;
-        clk.start(bs);
-        if (precision == SQBEM_MIXED) run_mixed(n, inst, prep, bs, results);
-        else run_fp64(n, inst, prep, bs, results);
-        clk.stop(bs);
-        const double secs = clk.seconds();
-        if (device_seconds) *device_seconds = secs;
+        Outputs o;
+        o.results = results;
+        kinematics_batch(n, inst, precision, o, device_seconds);
+    });
+}
+
+extern "C" int sqbem_kinematics_batch_tractions(int n, const sqbem_instance* inst, int precision, double* results,
+                                                double* const* f_sphere, double* const* f_tube,
+                                                double* device_seconds) {
+    return guarded([&] {
+        Outputs o;
+        o.results = results;
+        o.f_sphere = f_sphere;
+        o.f_tube = f_tube;
+        kinematics_batch(n, inst, precision, o, device_seconds);
     });
 }
 

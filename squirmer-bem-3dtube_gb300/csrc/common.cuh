@@ -56,6 +56,13 @@ bool kstats_on();
 void kstat_note(const std::string& note);
 int kstat_begin(cudaStream_t st);
 void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double bytes);
+// Work known only on the device when the launch is issued: n counters that the
+// caller copies (stream-ordered, before the timed launch) into pinned host
+// ints from kstat_pinned_ints; the launch is credited with sum w[i] * counts[i]
+// flops once its events have completed.
+int* kstat_pinned_ints(int n);
+void kstat_end_counted(int slot, const char* cls, cudaStream_t st, const int* counts, const double* w, int n,
+                       double bytes);
 #define TIMED_LAUNCH(cls, flops, bytes, kernel, grid, block, smem, stream, ...)          \
     do {                                                                                \
         const int _ks = ::sqbem::kstats_on() ? ::sqbem::kstat_begin(stream) : -1;      \
@@ -65,6 +72,14 @@ void kstat_end(int slot, const char* cls, cudaStream_t st, double flops, double 
 
 void require_device();
 void set_last_error(const char* msg);
+
+// Limits set by sqbem_set_limits: SM clock cycles a tensor-core GEMM role waits
+// on one mbarrier phase before it gives up (SQBEM_ERR_TIMEOUT), and the cap on
+// mixed-precision refinement steps (SQBEM_ERR_NOT_CONVERGED beyond it).
+constexpr long long DEFAULT_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+constexpr int DEFAULT_REFINE_MAX_IT = 30;
+long long gemm_wait_cycles();
+int refine_max_iterations();
 inline void set_last_error(const std::string& msg) { set_last_error(msg.c_str()); }
 
 // Run f; convert a failure into a status code and the thread's error message.

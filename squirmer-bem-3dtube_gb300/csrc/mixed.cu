@@ -792,16 +792,14 @@ __global__ void __cluster_dims__(TS_CL, 1, 1) __launch_bounds__(TS_THREADS)
     cl.sync();
 }
 
-void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
-                const std::vector<double*>& out, const std::vector<int>& n_true, int r, cudaStream_t st) {
-    if (g.empty()) return;
-    if (r < 1 || r > 2) fail(SQBEM_ERR_ARG, "trsv: 1 or 2 right-hand sides");
+namespace {
+template <int R>
+void trsv_launch(const std::vector<const MixedLU*>& g, const std::vector<TrsvIO>& io, int c0, int r, cudaStream_t st) {
     const int n = g[0]->n;
-    const size_t smem = trsv_smem(n, 2);
-    if (smem > 227 * 1024) fail(SQBEM_ERR_ARG, "trsv: %d unknowns exceed shared memory", n);
+    const size_t smem = trsv_smem(n, R);
     static std::once_flag attr;
     std::call_once(attr, [] {
-        CUDA_CHECK(cudaFuncSetAttribute(trsv_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        CUDA_CHECK(cudaFuncSetAttribute(trsv_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     });
     for (size_t i0 = 0; i0 < g.size(); i0 += MAXJOBS) {
         TrsvArgs a;
@@ -810,14 +808,38 @@ void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const do
         const int m = (int)std::min<size_t>(MAXJOBS, g.size() - i0);
         for (int k = 0; k < m; ++k) {
             const MixedLU& L = *g[i0 + k];
-            if (L.n != n) fail(SQBEM_ERR_ARG, "trsv: group members differ in size");
-            const int nt = n_true[i0 + k];
-            if (nt < 1 || nt > n) fail(SQBEM_ERR_ARG, "trsv: bad row count");
-            a.j[k] = {L.Rh.get(), L.Rl.get(), L.Li.get(), L.Ui.get(), in[i0 + k], nt, out[i0 + k], nt, nt};
+            const TrsvIO& q = io[i0 + k];
+            a.j[k] = {L.Rh.get(), L.Rl.get(), L.Li.get(), L.Ui.get(), q.in + (long long)c0 * q.ldi, q.ldi,
+                      q.out + (long long)c0 * q.ldo, q.ldo, q.n_true};
         }
         const double by = (double)m * ((double)n * n * 4.0 + 2.0 * n * r * 8.0);
-        TIMED_LAUNCH("trsv", 0.0, by, trsv_kernel<2>, m * TS_CL, TS_THREADS, smem, st, a);
+        TIMED_LAUNCH("trsv", 0.0, by, trsv_kernel<R>, m * TS_CL, TS_THREADS, smem, st, a);
     }
+}
+}  // namespace
+
+void trsv_group_io(const std::vector<const MixedLU*>& g, const std::vector<TrsvIO>& io, int r, cudaStream_t st) {
+    if (g.empty()) return;
+    if (r < 1 || r > 8 || io.size() != g.size()) fail(SQBEM_ERR_ARG, "trsv: 1 to 8 right-hand sides");
+    const int n = g[0]->n;
+    for (size_t k = 0; k < g.size(); ++k) {
+        if (g[k]->n != n) fail(SQBEM_ERR_ARG, "trsv: group members differ in size");
+        const int nt = io[k].n_true;
+        if (nt < 1 || nt > n || io[k].ldi < nt || io[k].ldo < nt) fail(SQBEM_ERR_ARG, "trsv: bad row count");
+    }
+    if (trsv_smem(n, 2) > 227 * 1024) fail(SQBEM_ERR_ARG, "trsv: %d unknowns exceed shared memory", n);
+    if (r > 2 && trsv_smem(n, 8) <= 227 * 1024) {
+        trsv_launch<8>(g, io, 0, r, st);
+        return;
+    }
+    for (int c0 = 0; c0 < r; c0 += 2) trsv_launch<2>(g, io, c0, std::min(2, r - c0), st);
+}
+
+void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
+                const std::vector<double*>& out, const std::vector<int>& n_true, int r, cudaStream_t st) {
+    std::vector<TrsvIO> io(g.size());
+    for (size_t k = 0; k < g.size(); ++k) io[k] = {in[k], n_true[k], out[k], n_true[k], n_true[k]};
+    trsv_group_io(g, io, r, st);
 }
 
 void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx) {

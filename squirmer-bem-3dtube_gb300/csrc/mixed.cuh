@@ -70,11 +70,20 @@ struct ConvJob {
 };
 void convert_group(const std::vector<ConvJob>& jobs, cudaStream_t st);
 
-// out <- A^{-1} in for every member's factor (n_true[k] x r, r <= 2, FP64 in and
-// out, leading dimension n_true[k]), one CTA per member: the block forward and
-// backward substitutions with the split factor and the block inverses, for
-// refinement corrections.
+// out <- A^{-1} in for every member's factor (n_true[k] x r, r <= 8, FP64 in and
+// out, leading dimension n_true[k]), one 4-CTA cluster per member: the block
+// forward and backward substitutions with the split factor and the block
+// inverses, for refinement corrections and few-column solves.
 void trsv_group(const std::vector<const MixedLU*>& g, const std::vector<const double*>& in,
                 const std::vector<double*>& out, const std::vector<int>& n_true, int r, cudaStream_t st);
+// The same with explicit leading dimensions of in and out per member.
+struct TrsvIO {
+    const double* in = nullptr;
+    long long ldi = 0;
+    double* out = nullptr;
+    long long ldo = 0;
+    int n_true = 0;
+};
+void trsv_group_io(const std::vector<const MixedLU*>& g, const std::vector<TrsvIO>& io, int r, cudaStream_t st);
 
 }  // namespace sqbem

@@ -1,10 +1,11 @@
 // mixed_solver.cu -- the SQBEM_MIXED swimmer path over groups of instances.
 //
 // Build (per group): FP32 assembly of every block (FP64 relative vectors, FP64
-// 448-point and self integrals); T^{-1} and G_s^{-1} by the certified LU and the
-// LU solve of the identity on the tensor cores; Y = T^{-1}[B | Ct] and
-// [G_s | G_c] = [E | Cs] - D Y as grouped tensor-core GEMMs; Z = G_s^{-1} G_c
-// and S6 = F Z in FP64, S6 inverted on the host (6 x 6).
+// 448-point and self integrals); T's certified LU on the tensor cores (and, for a
+// tube shared by many swimmers, T^{-1} by the LU solve of the identity);
+// Y = T^{-1}[B | Ct] and [G_s | G_c] = [E | Cs] - D Y as grouped tensor-core
+// GEMMs; G_s's certified LU; Z = G_s^{-1} G_c by block substitutions and
+// S6 = F Z in FP64, S6 inverted on the device (6 x 6, FP64).
 // Solve: iterative refinement of the full system in FP64 (see mixed_solver.cuh).
 #include <cuda_runtime.h>
 
@@ -66,12 +67,27 @@ void check_ctx(const MixedCtx& cx, const char* what) {
     if (read_int(cx.err, cx.st)) fail(SQBEM_ERR_TIMEOUT, "%s: a bounded wait in the tensor-core GEMM expired", what);
     const int f = read_int(cx.flag, cx.st);
     if (f & 2) fail(SQBEM_ERR_SINGULAR, "%s failed: zero pivot", what);
+    if (f & 4) fail(SQBEM_ERR_SINGULAR, "dgesv failed (rigid-body 6 x 6 system)");
     if (f & 1)
         fail(SQBEM_ERR_SINGULAR, "%s: partial pivoting would exchange rows; the mixed LU does not pivot", what);
 }
 
-// 6 x 6 inverse by Gauss-Jordan with partial pivoting (FP64, host)
-bool invert6(const double* A, double* Ai) {
+// S6^{-1} for every member: Gauss-Jordan elimination with partial pivoting in
+// FP64, one thread per 6 x 6 system (FP64 on the GPU for the rigid-body solve;
+// round-to-nearest operations without contraction, so the result does not
+// depend on the compiler's FMA choices).  A zero pivot sets bit 2 of *flag.
+constexpr int INV6_MAX = 64;
+struct Inv6Args {
+    int n;
+    int* flag;
+    const double* S;      // member k at S + 36 k, column-major 6 x 6
+    double* Si[INV6_MAX];
+};
+
+__global__ void invert6_kernel(const __grid_constant__ Inv6Args args) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= args.n) return;
+    const double* A = args.S + 36 * (long long)k;
     double a[6][12];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) {
@@ -81,21 +97,28 @@ bool invert6(const double* A, double* Ai) {
     for (int c = 0; c < 6; ++c) {
         int p = c;
         for (int r = c + 1; r < 6; ++r)
-            if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
-        if (!(std::fabs(a[p][c]) > 0)) return false;
+            if (fabs(a[r][c]) > fabs(a[p][c])) p = r;
+        if (!(fabs(a[p][c]) > 0)) {
+            atomicOr(args.flag, 4);
+            return;
+        }
         if (p != c)
-            for (int j = 0; j < 12; ++j) std::swap(a[p][j], a[c][j]);
+            for (int j = 0; j < 12; ++j) {
+                const double t = a[p][j];
+                a[p][j] = a[c][j];
+                a[c][j] = t;
+            }
         const double d = a[c][c];
-        for (int j = 0; j < 12; ++j) a[c][j] /= d;
+        for (int j = 0; j < 12; ++j) a[c][j] = __ddiv_rn(a[c][j], d);
         for (int r = 0; r < 6; ++r)
             if (r != c) {
                 const double f = a[r][c];
-                for (int j = 0; j < 12; ++j) a[r][j] -= f * a[c][j];
+                for (int j = 0; j < 12; ++j) a[r][j] = __dsub_rn(a[r][j], __dmul_rn(f, a[c][j]));
             }
     }
+    double* out = args.Si[k];
     for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) Ai[i + 6 * j] = a[i][6 + j];
-    return true;
+        for (int j = 0; j < 6; ++j) out[i + 6 * j] = a[i][6 + j];
 }
 
 CopyJob cp32_64(const float* s, long long lds, double* d, long long ldd, int rows, int cols) {
@@ -387,43 +410,49 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
     }
     mixed_lu_factor(gl, cx);
     check_ctx(cx, "dgetrf (mixed Schur factor)");
-    std::vector<float*> inv;
+    // keep G_s's factor (the solves read only the split factor and the block
+    // inverses); Z = G_s^{-1} G_c by block substitutions, then S6 = F Z in FP64,
+    // S6 inverted on the device
+    std::vector<const MixedLU*> gf;
     for (size_t k = 0; k < G; ++k) {
-        MixedSwimmer& M = sw[k]->mx;
-        M.Gi.alloc((size_t)M.nsp * M.nsp, cx.st);
-        inv.push_back(M.Gi.get());
+        glu[k].A.release();
+        glu[k].Ch.release();
+        glu[k].Cl.release();
+        sw[k]->mx.glu = std::make_unique<MixedLU>(std::move(glu[k]));
+        gf.push_back(sw[k]->mx.glu.get());
     }
-    invert_group(gl, inv, {}, {}, cx);
-    // Z = G_s^{-1} G_c and S6 = F Z in FP64; S6 inverted on the host
     std::vector<DevBuf<double>> gc64(G);
     DevBuf<double> s6((size_t)36 * G, cx.st);
+    std::vector<TrsvIO> zio(G);
     for (size_t k = 0; k < G; ++k) {
         MixedSwimmer& M = sw[k]->mx;
         gc64[k].alloc((size_t)M.ns * 6, cx.st);
         cj.push_back(cp32_64(Gc[k].get(), M.ns, gc64[k].get(), M.ns, M.ns, 6));
         M.Z64.alloc((size_t)M.ns * 6, cx.st);
-        mj.push_back(mv32(M.Gi.get(), M.nsp, M.ns, M.ns, gc64[k].get(), M.ns, 6, M.Z64.get(), M.ns, 1.0, 0.0));
+        zio[k] = {gc64[k].get(), M.ns, M.Z64.get(), M.ns, M.ns};
     }
     copy_group(cj, cx.st);
     cj.clear();
-    matvec_group(mj, cx.st);
-    mj.clear();
+    trsv_group_io(gf, zio, 6, cx.st);
     for (size_t k = 0; k < G; ++k) {
         MixedSwimmer& M = sw[k]->mx;
         mj.push_back(mv64(M.F.get(), 6, 6, M.ns, M.Z64.get(), M.ns, 6, s6.get() + 36 * k, 6, 1.0, 0.0));
     }
     matvec_group(mj, cx.st);
     mj.clear();
-    std::vector<double> h6(36 * G);
-    s6.download(h6.data(), h6.size());
-    check_ctx(cx, "mixed Schur inverse");
-    for (size_t k = 0; k < G; ++k) {
-        double inv6[36];
-        if (!invert6(h6.data() + 36 * k, inv6)) fail(SQBEM_ERR_SINGULAR, "dgesv failed (rigid-body 6 x 6 system)");
-        MixedSwimmer& M = sw[k]->mx;
-        M.S6i.alloc(36, cx.st);
-        M.S6i.upload(inv6, 36);
+    for (size_t k0 = 0; k0 < G; k0 += INV6_MAX) {
+        Inv6Args a;
+        a.n = (int)std::min<size_t>(INV6_MAX, G - k0);
+        a.flag = cx.flag;
+        a.S = s6.get() + 36 * k0;
+        for (int k = 0; k < a.n; ++k) {
+            MixedSwimmer& M = sw[k0 + k]->mx;
+            M.S6i.alloc(36, cx.st);
+            a.Si[k] = M.S6i.get();
+        }
+        LAUNCH(invert6_kernel, 1, INV6_MAX, 0, cx.st, a);
     }
+    check_ctx(cx, "mixed Schur inverse");
 }
 
 // ---------------------------------------------------------------- refinement
@@ -529,8 +558,9 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     const std::vector<double> r0 = norms();
     int it = 0;
     double worst = 0;
+    const int max_it = refine_max_iterations();
     for (size_t k = 0; k < G * r; ++k) worst = std::max(worst, r0[k] > 0 ? 1.0 : 0.0);
-    for (it = 1; it <= REFINE_MAX_IT && worst > REFINE_TOL; ++it) {
+    for (it = 1; it <= max_it && worst > REFINE_TOL; ++it) {
         // (a) y_t = T^{-1} r_t   (b) r_s' = r_s - D y_t
         for (size_t k = 0; k < G; ++k) {
             MixedSwimmer& M = sw[k]->mx;
@@ -565,13 +595,18 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             matvec_group(mj, cx.st);
             mj.clear();
         }
-        // (c) v = G_s^{-1} r_s', written into the top of d_sw
-        for (size_t k = 0; k < G; ++k) {
-            MixedSwimmer& M = sw[k]->mx;
-            mj.push_back(mv32(M.Gi.get(), M.nsp, M.ns, M.ns, W[k].rsp.get(), M.ns, r, W[k].dsw.get(), M.nc, 1.0, 0.0));
+        // (c) v = G_s^{-1} r_s' by block substitutions with G_s's factor, written
+        // into the top of d_sw
+        {
+            std::vector<const MixedLU*> gf;
+            std::vector<TrsvIO> io;
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                gf.push_back(M.glu.get());
+                io.push_back({W[k].rsp.get(), M.ns, W[k].dsw.get(), M.nc, M.ns});
+            }
+            trsv_group_io(gf, io, r, cx.st);
         }
-        matvec_group(mj, cx.st);
-        mj.clear();
         if (prescribed) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
@@ -641,7 +676,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     *residual = worst;
     if (worst > REFINE_TOL)
         fail(SQBEM_ERR_NOT_CONVERGED, "mixed refinement reached relative residual %.3e after %d iterations", worst,
-             REFINE_MAX_IT);
+             max_it);
 }
 
 }  // namespace sqbem

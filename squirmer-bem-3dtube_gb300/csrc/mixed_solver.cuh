@@ -8,9 +8,11 @@
 // preconditioner is the Schur elimination on split-BF16 tensor cores: the LU of
 // T; Y = T^{-1}[B | Ct] by the LU solves (a tube serving one swimmer) or as one
 // GEMM with an explicit T^{-1} (a tube shared by many swimmers); G = [E | Cs] -
-// D Y, G_s^{-1} formed explicitly, Z = G_s^{-1} G_c and the 6 x 6 rigid-body
-// system S6 = F Z solved in FP64.  Every refinement step is one triangular solve
-// with T's factor (or a product with T^{-1}) and a handful of HBM-bound products.
+// D Y factored (its inverse is never formed: Z = G_s^{-1} G_c and every
+// refinement step's G_s^{-1} r come from block substitutions with the factor),
+// and the 6 x 6 rigid-body system S6 = F Z solved in FP64.  Every refinement
+// step is one triangular solve with T's factor (or a product with T^{-1}), one
+// with G_s's factor and a handful of HBM-bound products.
 // Iterative refinement on the full system, residuals accumulated in FP64,
 // stops when the relative residual reaches REFINE_TOL.
 #pragma once
@@ -31,7 +33,7 @@ namespace sqbem {
 // each contracting the residual ~3e-5; the U, Omega error is the same as at
 // 1e-11 to three digits).
 constexpr double REFINE_TOL = 1e-8;
-constexpr int REFINE_MAX_IT = 30;
+// The cap on refinement steps is refine_max_iterations() (sqbem_set_limits).
 
 struct MixedTube {
     int nt = 0, ntp = 0;          // 3 Nt and its multiple of 128
@@ -55,7 +57,8 @@ struct MixedSwimmer {
     DevBuf<float> Ct, Cs;         // nt x 6, ns x 6
     DevBuf<float> Y;              // T^{-1} [B | Ct], nt x nc, leading dimension ldY
     long long ldY = 0;            // nt (explicit T^{-1}) or the padded ntp (the LU solve's buffer)
-    DevBuf<float> Gi;             // G_s^{-1}, nsp x nsp column-major
+    std::unique_ptr<MixedLU> glu; // G_s's split factor and diagonal-block inverses (A, Ch, Cl released):
+                                  // G_s^{-1} is applied by block substitutions (trsv_group_io)
     DevBuf<double> Z64;           // G_s^{-1} G_c (ns x 6), FP64
     DevBuf<double> F;             // 6 x ns, column-major (ld 6), unscaled
     DevBuf<double> S6i;           // (F Z)^{-1}, 6 x 6 column-major

@@ -87,6 +87,20 @@ struct sqbem_tube {
 std::vector<double> squirmer_slip_host(const std::vector<sqbem::PanelRec>& S, const double* xc, const double* e,
                                        double B1, double B2);
 
+namespace sqbem {
+// The same slip field on the device, bit-identical to squirmer_slip_host: for
+// every job, out[0 .. 3 Ns) = the B1 = 1 mode and out[3 Ns .. 6 Ns) = the B2 = 1
+// mode at the centroids of the Ns panel records (one grouped launch).
+struct SlipJob {
+    const PanelRec* rec = nullptr;
+    int Ns = 0;
+    double xc[3] = {0, 0, 0};
+    double e[3] = {0, 0, 1};
+    double* out = nullptr;
+};
+void slip_modes_group(const std::vector<SlipJob>& jobs, cudaStream_t st);
+}  // namespace sqbem
+
 // SwimmerSolver, src/swimmer.hpp:83-289
 struct sqbem_swimmer {
     sqbem::Stream st;

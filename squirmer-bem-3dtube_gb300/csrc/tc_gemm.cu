@@ -15,18 +15,23 @@
 //              optional split-BF16 stores, then release the accumulator.
 // Two accumulators let the epilogue of tile t overlap the MMAs of tile t + 1.
 // Tiles of all problems are enumerated in one list; CTA b takes tiles b,
-// b + gridDim, ...  Every mbarrier wait is bounded (about 2 s of SM clock); on
-// expiry the kernel raises *err, drains its own copies and MMAs, frees its TMEM
-// and returns.
+// b + gridDim, ...  Every mbarrier wait is bounded (sqbem_set_limits; by default
+// about 2 s of SM clock); on expiry the kernel raises *err, drains its own
+// copies and MMAs, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <dlfcn.h>
+
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -36,14 +41,32 @@ namespace sqbem {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int STAGES = 3;
-constexpr int TILE_BYTES = BM * BK * 2;            // 16 KB (A and B tiles alike)
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;        // A_hi, A_lo, B_hi, B_lo
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int TMEM_COLS = 256;
+constexpr int BM = 128, BK = 64;
+constexpr int A_TILE = BM * BK * 2;  // 16 KB per A plane of a stage
 constexpr int NTHREADS = 192;
-constexpr long long WAIT_CYCLES = 4000000000LL;   // ~2 s at 2 GHz
+
+// Tile variants of the kernel; the autotuner (tune_gemm.py) picks one per shape
+// class of the launches.  A stage holds A_hi, A_lo (128 x 64 each) and B_hi, B_lo
+// (BN x 64 each); the two TMEM accumulators take 2 BN columns.
+template <int BN_, int STAGES_>
+struct Tile {
+    static constexpr int BN = BN_, STAGES = STAGES_;
+    static constexpr int B_TILE = BN * BK * 2;
+    static constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+    static constexpr int TMEM_COLS = 2 * BN;
+    // instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM
+    static constexpr uint32_t IDESC =
+        (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+    static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+    static_assert(TMEM_COLS <= 512, "tensor memory columns");
+};
+using TileA = Tile<128, 3>;  // variant 0: 128 x 128 tiles, 3 stages of 64 KB
+using TileB = Tile<256, 2>;  // variant 1: 128 x 256 tiles, 2 stages of 96 KB
+// Waits that keep the CTA alive until its own copies and MMAs have landed (before
+// shared memory and TMEM are given up) use the default limit, never the
+// caller's: leaving earlier would let a copy write into released memory.
+constexpr long long DRAIN_CYCLES = DEFAULT_WAIT_CYCLES;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -73,18 +96,19 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase of the given parity; false (and *err = 1) on expiry
-// or if another role already gave up.  The error flag (a global load) and the
-// clock are polled only every 64 tries: a global load inside every poll would
-// delay the reaction to a completed phase by an L2 round trip.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+// Bounded wait for the phase of the given parity; false (and *err = 1) after
+// `limit` SM cycles or if another role already gave up.  The error flag (a
+// global load) and the clock are polled only every 64 tries: a global load
+// inside every poll would delay the reaction to a completed phase by an L2 round
+// trip.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, long long limit) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     for (int it = 1;; ++it) {
         if (mbar_try(bar, parity)) return true;
         if ((it & 63) == 0) {
             if (*(volatile int*)err) return false;
-            if (clock64() - t0 > WAIT_CYCLES) {
+            if (clock64() - t0 > limit) {
                 atomicExch(err, 1);
                 return false;
             }
@@ -109,15 +133,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
 }
 
-// Instruction descriptor: D = F32, A = B = BF16, both K-major, N = BN, M = BM.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(d_tmem), "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
@@ -155,6 +177,9 @@ constexpr int MAXP = SQBEM_TC_MAXP;
 struct KArgs {
     int nprob;
     int total_tiles;
+    long long wait;  // SM cycles per bounded wait (gemm_wait_cycles())
+    int stall;       // test hook (sqbem_test_gemm_stall): CTA 0's MMA issuer first waits on a
+                     // barrier that nothing arrives on, so that wait runs out
     int* err;
     int* flag;
     TcProblem probs[MAXP];
@@ -171,7 +196,10 @@ __device__ __forceinline__ int find_problem(const TcProblem* probs, int nprob, i
     return lo;
 }
 
+template <class T>
 __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_constant__ KArgs args) {
+    constexpr int BN = T::BN, STAGES = T::STAGES, STAGE_BYTES = T::STAGE_BYTES, B_TILE = T::B_TILE;
+    constexpr int TMEM_COLS = T::TMEM_COLS;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -179,8 +207,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
     const uint32_t tfull0 = smem_u32(bars + 2 * STAGES), tempty0 = smem_u32(bars + 2 * STAGES + 2);
     const uint32_t done_bar = smem_u32(bars + 2 * STAGES + 4);
     uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 5);
+    const uint32_t stall_bar = smem_u32(bars + 2 * STAGES + 6);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int* err = args.err;
+    const long long wait = args.wait;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -192,6 +222,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             mbar_init(tempty0 + 8 * a, 128);
         }
         mbar_init(done_bar, 1);
+        mbar_init(stall_bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -223,16 +254,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             const int local = t - P.tile_start;
             const int tm = local / P.tiles_n, tn = local % P.tiles_n;
             const int nkb = (P.K + BK - 1) / BK;
+            const bool three = P.products != 2;  // two products: A_lo is not read
             bool ok = true;
             for (int kb = 0; kb < nkb; ++kb) {
-                if (!mbar_wait(empty0 + 8 * s, ph ^ 1, err)) { ok = false; break; }
+                if (!mbar_wait(empty0 + 8 * s, ph ^ 1, err, wait)) { ok = false; break; }
                 const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
                 const uint32_t fb = full0 + 8 * s;
-                mbar_expect_tx(fb, STAGE_BYTES);
+                mbar_expect_tx(fb, three ? STAGE_BYTES : STAGE_BYTES - A_TILE);
                 tma_load_2d(st, m + 0, kb * BK, tm * BM, fb);
-                tma_load_2d(st + TILE_BYTES, m + 1, kb * BK, tm * BM, fb);
-                tma_load_2d(st + 2 * TILE_BYTES, m + 2, kb * BK, tn * BN, fb);
-                tma_load_2d(st + 3 * TILE_BYTES, m + 3, kb * BK, tn * BN, fb);
+                if (three) tma_load_2d(st + A_TILE, m + 1, kb * BK, tm * BM, fb);
+                tma_load_2d(st + 2 * A_TILE, m + 2, kb * BK, tn * BN, fb);
+                tma_load_2d(st + 2 * A_TILE + B_TILE, m + 3, kb * BK, tn * BN, fb);
                 armed[s] += 1;
                 if (++s == STAGES) { s = 0; ph ^= 1; }
             }
@@ -243,7 +275,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
             if (armed[q] > 0) {
                 const uint32_t par = (uint32_t)((armed[q] - 1) & 1);
                 const long long t0 = clock64();
-                while (!mbar_try(full0 + 8 * q, par) && clock64() - t0 < WAIT_CYCLES) {
+                while (!mbar_try(full0 + 8 * q, par) && clock64() - t0 < DRAIN_CYCLES) {
                 }
             }
     } else if (warp == 1 && lane == 0) {
@@ -252,25 +284,28 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
         uint32_t ph = 0;
         int acc = 0;
         uint32_t aph = 0;
-        for (int t = blockIdx.x; t < args.total_tiles; t += gridDim.x) {
+        // the test hook's wait: nothing arrives on stall_bar, so it ends by the limit
+        const bool stalled = args.stall && blockIdx.x == 0 && !mbar_wait(stall_bar, 0, err, wait);
+        for (int t = stalled ? args.total_tiles : blockIdx.x; t < args.total_tiles; t += gridDim.x) {
             const int p = find_problem(args.probs, args.nprob, t);
             const int nkb = (args.probs[p].K + BK - 1) / BK;
-            if (!mbar_wait(tempty0 + 8 * acc, aph ^ 1, err)) break;
+            const bool three = args.probs[p].products != 2;
+            if (!mbar_wait(tempty0 + 8 * acc, aph ^ 1, err, wait)) break;
             tc_fence_after();
             const uint32_t d = tmem_base + (uint32_t)(acc * BN);
             bool ok = true;
             for (int kb = 0; kb < nkb; ++kb) {
-                if (!mbar_wait(full0 + 8 * s, ph, err)) { ok = false; break; }
+                if (!mbar_wait(full0 + 8 * s, ph, err, wait)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-                const uint64_t ah = smem_desc(st), al = smem_desc(st + TILE_BYTES);
-                const uint64_t bh = smem_desc(st + 2 * TILE_BYTES), bl = smem_desc(st + 3 * TILE_BYTES);
+                const uint64_t ah = smem_desc(st), al = smem_desc(st + A_TILE);
+                const uint64_t bh = smem_desc(st + 2 * A_TILE), bl = smem_desc(st + 2 * A_TILE + B_TILE);
 #pragma unroll
                 for (int k = 0; k < BK / 16; ++k) {
                     const uint64_t off = (uint64_t)(k * 32) >> 4;  // 16 BF16 = 32 bytes along K
-                    mma_bf16(d, ah + off, bh + off, (kb > 0 || k > 0) ? 1u : 0u);
-                    mma_bf16(d, ah + off, bl + off, 1u);
-                    mma_bf16(d, al + off, bh + off, 1u);
+                    mma_bf16(d, ah + off, bh + off, T::IDESC, (kb > 0 || k > 0) ? 1u : 0u);
+                    mma_bf16(d, ah + off, bl + off, T::IDESC, 1u);
+                    if (three) mma_bf16(d, al + off, bh + off, T::IDESC, 1u);
                 }
                 mma_commit(empty0 + 8 * s);
                 if (++s == STAGES) { s = 0; ph ^= 1; }
@@ -282,7 +317,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
         // all MMAs issued by this CTA complete before TMEM is released
         mma_commit(done_bar);
         const long long t0 = clock64();
-        while (!mbar_try(done_bar, 0) && clock64() - t0 < WAIT_CYCLES) {
+        while (!mbar_try(done_bar, 0) && clock64() - t0 < DRAIN_CYCLES) {
         }
     } else if (warp >= 2) {
         // ---------------- epilogue
@@ -325,7 +360,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gemm_kernel(const __grid_const
                 for (int j = 0; j < 32; ++j) cnext[j] = j < cnt ? c[(long long)j * ccs] : 0.f;
             };
             if (rd) load_c(0);
-            if (!mbar_wait(tfull0 + 8 * acc, aph, err)) break;
+            if (!mbar_wait(tfull0 + 8 * acc, aph, err, wait)) break;
             tc_fence_after();
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -436,14 +471,14 @@ void get_encode() {
 }
 
 // Tensor map of a K-major BF16 plane: rows x k, row pitch ld elements, boxes of
-// 128 rows x 64 k with 128-byte swizzle, zero fill outside the matrix.
-CUtensorMap make_map(const bf16* base, int rows, int k, long long ld) {
+// box_rows rows x 64 k with 128-byte swizzle, zero fill outside the matrix.
+CUtensorMap make_map(const bf16* base, int rows, int k, long long ld, int box_rows) {
     if (((uintptr_t)base & 15) != 0 || (ld * 2) % 16 != 0 || rows <= 0 || k <= 0)
         fail(SQBEM_ERR_ARG, "tensor map: misaligned operand (ld %lld)", ld);
     CUtensorMap m;
     cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
-    cuuint32_t box[2] = {BK, BM};
+    cuuint32_t box[2] = {BK, (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -454,6 +489,7 @@ CUtensorMap make_map(const bf16* base, int rows, int k, long long ld) {
 
 int g_num_sms = 0;
 std::once_flag g_sms_once;
+std::atomic<int> g_test_stalls{0};
 
 }  // namespace
 
@@ -464,16 +500,101 @@ void split_convert(const float* src, long long s_rs, long long s_cs, int rows, i
            d_cs);
 }
 
+// ---------------------------------------------------------------- variants and tuning
+namespace {
+struct VariantInfo {
+    int bn, stages, smem;
+    void (*kernel)(KArgs);
+};
+const VariantInfo kVariants[] = {
+    {TileA::BN, TileA::STAGES, TileA::SMEM_BYTES, tc_gemm_kernel<TileA>},
+    {TileB::BN, TileB::STAGES, TileB::SMEM_BYTES, tc_gemm_kernel<TileB>},
+};
+constexpr int NVARIANTS = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+
+// The tuning table: rows "kmax nmax variant"; a launch takes the first row with
+// K <= kmax and N <= nmax (its largest problem's K and N).  Read once from
+// SQBEM_TC_TABLE or, by default, tuning/tc_gemm.txt next to the library's lib/
+// folder; without a table every launch takes variant 0.  SQBEM_TC_VARIANT forces
+// one variant for every launch (used by the tuner).
+struct TableRow {
+    int kmax, nmax, variant;
+};
+std::vector<TableRow> g_table;
+int g_forced = -1;
+std::once_flag g_table_once;
+
+std::string default_table_path() {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void*>(&tc_gemm_variants), &info) && info.dli_fname) {
+        std::string lib(info.dli_fname);
+        const size_t slash = lib.rfind('/');
+        const std::string dir = slash == std::string::npos ? "." : lib.substr(0, slash);
+        return dir + "/../tuning/tc_gemm.txt";
+    }
+    return "";
+}
+
+void load_table() {
+    std::call_once(g_table_once, [] {
+        if (const char* f = std::getenv("SQBEM_TC_VARIANT")) {
+            const int v = std::atoi(f);
+            if (v >= 0 && v < NVARIANTS) g_forced = v;
+        }
+        const char* env = std::getenv("SQBEM_TC_TABLE");
+        const std::string path = env ? std::string(env) : default_table_path();
+        FILE* fp = path.empty() ? nullptr : std::fopen(path.c_str(), "r");
+        if (!fp) return;
+        char line[256];
+        while (std::fgets(line, sizeof line, fp)) {
+            TableRow r;
+            if (line[0] == '#') continue;
+            if (std::sscanf(line, "%d %d %d", &r.kmax, &r.nmax, &r.variant) == 3 && r.variant >= 0 &&
+                r.variant < NVARIANTS)
+                g_table.push_back(r);
+        }
+        std::fclose(fp);
+    });
+}
+}  // namespace
+
+int tc_gemm_variants() { return NVARIANTS; }
+
+void tc_gemm_variant_info(int v, int* bn, int* stages) {
+    if (v < 0 || v >= NVARIANTS) fail(SQBEM_ERR_ARG, "tc_gemm: no variant %d", v);
+    if (bn) *bn = kVariants[v].bn;
+    if (stages) *stages = kVariants[v].stages;
+}
+
+int tc_gemm_choose(int kmax, int nmax) {
+    load_table();
+    if (g_forced >= 0) return g_forced;
+    for (const TableRow& r : g_table)
+        if (kmax <= r.kmax && nmax <= r.nmax) return r.variant;
+    return 0;
+}
+
 void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperands>& ops, int* err, int* flag,
-             cudaStream_t st) {
+             cudaStream_t st, int variant) {
     if (probs_in.size() != ops.size()) fail(SQBEM_ERR_ARG, "tc_gemm: operand count");
     get_encode();
     std::call_once(g_sms_once, [] {
         int dev = 0;
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-        CUDA_CHECK(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        for (const VariantInfo& v : kVariants)
+            CUDA_CHECK(cudaFuncSetAttribute(v.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v.smem));
     });
+    if (variant < 0) {
+        int kmax = 0, nmax = 0;
+        for (const TcProblem& P : probs_in) {
+            kmax = std::max(kmax, P.K);
+            nmax = std::max(nmax, P.N);
+        }
+        variant = tc_gemm_choose(kmax, nmax);
+    }
+    if (variant >= NVARIANTS) fail(SQBEM_ERR_ARG, "tc_gemm: no variant %d", variant);
+    const VariantInfo& V = kVariants[variant];
     KArgs a;
     auto h0 = std::chrono::steady_clock::now();
     auto flush = [&](double flops, double bytes) {
@@ -488,24 +609,31 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
                 mn = std::max(mn, a.probs[q].N);
                 mk = std::max(mk, a.probs[q].K);
             }
-            char note[128];
-            std::snprintf(note, sizeof note, "nprob=%d tiles=%d grid=%d M=%d N=%d K=%d host_us=%.1f", a.nprob,
-                          a.total_tiles, grid, mm, mn, mk, host_us);
+            char note[160];
+            std::snprintf(note, sizeof note, "nprob=%d tiles=%d grid=%d M=%d N=%d K=%d variant=%d host_us=%.1f",
+                          a.nprob, a.total_tiles, grid, mm, mn, mk, variant, host_us);
             kstat_note(note);
         }
-        TIMED_LAUNCH("tc_gemm", flops, bytes, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, st, a);
+        TIMED_LAUNCH("tc_gemm", flops, bytes, V.kernel, grid, NTHREADS, V.smem, st, a);
         h0 = std::chrono::steady_clock::now();
     };
     a.nprob = 0;
     a.total_tiles = 0;
     a.err = err;
     a.flag = flag;
+    a.wait = gemm_wait_cycles();
+    a.stall = 0;
+    int stalls = g_test_stalls.load();
+    while (stalls > 0 && !g_test_stalls.compare_exchange_weak(stalls, stalls - 1)) {
+    }
+    if (stalls > 0) a.stall = 1;  // this call takes one requested stall
     double flops = 0, bytes = 0;
     for (size_t i = 0; i < probs_in.size(); ++i) {
         TcProblem P = probs_in[i];
         const TcOperands& o = ops[i];
         if (P.M <= 0 || P.N <= 0) continue;
         if (P.K <= 0) fail(SQBEM_ERR_ARG, "tc_gemm: K must be positive");
+        if (P.products != 2 && P.products != 3) fail(SQBEM_ERR_ARG, "tc_gemm: 2 or 3 products");
         if (o.A.rows < P.M || o.A.k < P.K || o.B.rows < P.N || o.B.k < P.K)
             fail(SQBEM_ERR_ARG, "tc_gemm: operand smaller than the problem");
         if (a.nprob == MAXP) {
@@ -514,18 +642,19 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
             a.total_tiles = 0;
             flops = bytes = 0;
         }
-        P.tiles_n = ceil_div(P.N, BN);
+        P.tiles_n = ceil_div(P.N, V.bn);
         P.tile_start = a.total_tiles;
         a.total_tiles += ceil_div(P.M, BM) * P.tiles_n;
         // maps cover exactly the problem's extent: rows beyond M / N and k beyond K read as zero
-        a.maps[4 * a.nprob + 0] = make_map(o.A.hi, P.M, P.K, o.A.ld);
-        a.maps[4 * a.nprob + 1] = make_map(o.A.lo, P.M, P.K, o.A.ld);
-        a.maps[4 * a.nprob + 2] = make_map(o.B.hi, P.N, P.K, o.B.ld);
-        a.maps[4 * a.nprob + 3] = make_map(o.B.lo, P.N, P.K, o.B.ld);
+        a.maps[4 * a.nprob + 0] = make_map(o.A.hi, P.M, P.K, o.A.ld, BM);
+        a.maps[4 * a.nprob + 1] = P.products == 2 ? a.maps[4 * a.nprob] : make_map(o.A.lo, P.M, P.K, o.A.ld, BM);
+        a.maps[4 * a.nprob + 2] = make_map(o.B.hi, P.N, P.K, o.B.ld, V.bn);
+        a.maps[4 * a.nprob + 3] = make_map(o.B.lo, P.N, P.K, o.B.ld, V.bn);
         a.probs[a.nprob++] = P;
-        // tensor-pipe work: three BF16 products (hi*hi, hi*lo, lo*hi) per element product
-        flops += 3.0 * 2.0 * P.M * P.N * P.K;
-        bytes += 4.0 * ((double)P.M * P.K + (double)P.K * P.N) + 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
+        // tensor-pipe work: two or three BF16 products per element product
+        flops += P.products * 2.0 * P.M * P.N * P.K;
+        bytes += ((P.products == 2 ? 2.0 : 4.0) * P.M * P.K + 4.0 * P.K * P.N) +
+                 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
     }
     flush(flops, bytes);
 }
@@ -534,40 +663,143 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
 
 using namespace sqbem;
 
+namespace sqbem {
+namespace {
+
+// A stream of its own for one host-facing call, destroyed on every exit path.
+struct CallStream {
+    cudaStream_t s = nullptr;
+    CallStream() { CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~CallStream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+};
+
+void gemm_host(int variant, int products, int M, int N, int K, float alpha, const float* A, int lda, const float* B,
+               int ldb, float beta, float* C, int ldc) {
+    if (M < 0 || N < 0 || K <= 0 || !A || !B || !C || lda < M || ldb < K || ldc < M ||
+        (products != 2 && products != 3) || variant < -1 || variant >= NVARIANTS)
+        fail(SQBEM_ERR_ARG, "gemm_mixed: bad arguments");
+    if (M == 0 || N == 0) return;
+    require_device();
+    CallStream cs;
+    const cudaStream_t st = cs.s;
+    const long long ld = pad_ld(K);
+    DevBuf<float> dA((size_t)lda * K, st), dB((size_t)ldb * N, st), dC((size_t)ldc * N, st);
+    DevBuf<bf16> ah((size_t)M * ld, st), al((size_t)M * ld, st), bh((size_t)N * ld, st), bl((size_t)N * ld, st);
+    DevBuf<int> err(1, st);
+    err.zero();
+    dA.upload(A, (size_t)lda * K);
+    dB.upload(B, (size_t)ldb * N);
+    dC.upload(C, (size_t)ldc * N);
+    // A (col-major M x K) -> K-major rows; B (col-major K x N) -> K-major columns
+    split_convert(dA.get(), 1, lda, M, K, ah.get(), al.get(), ld, 1, st);
+    split_convert(dB.get(), 1, ldb, K, N, bh.get(), bl.get(), 1, ld, st);
+    TcProblem P;
+    P.M = M; P.N = N; P.K = K; P.alpha = alpha; P.beta = beta;
+    P.C = dC.get(); P.c_rs = 1; P.c_cs = ldc;
+    P.products = products;
+    TcOperands o;
+    o.A = {ah.get(), al.get(), M, K, ld};
+    o.B = {bh.get(), bl.get(), N, K, ld};
+    tc_gemm({P}, {o}, err.get(), nullptr, st, variant);
+    int h_err = 0;
+    err.download(&h_err, 1);
+    dC.download(C, (size_t)ldc * N);
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    if (h_err) fail(SQBEM_ERR_TIMEOUT, "gemm_mixed: a bounded wait in the tensor-core GEMM expired");
+}
+
+// deterministic pseudo-random BF16 planes in [-1, 1) for the timing entry point
+__global__ void fill_planes_kernel(bf16* p, size_t n, unsigned seed) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned h = (unsigned)i * 2654435761u ^ seed;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    p[i] = __float2bfloat16_rn((float)(h & 0xffff) / 32768.f - 1.f);
+}
+
+}  // namespace
+}  // namespace sqbem
+
 extern "C" int sqbem_gemm_mixed(int M, int N, int K, float alpha, const float* A, int lda, const float* B, int ldb,
                                 float beta, float* C, int ldc) {
+    return guarded([&] { gemm_host(-1, 3, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc); });
+}
+
+extern "C" int sqbem_gemm_mixed_ex(int variant, int products, int M, int N, int K, float alpha, const float* A,
+                                   int lda, const float* B, int ldb, float beta, float* C, int ldc) {
+    return guarded([&] { gemm_host(variant, products, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc); });
+}
+
+extern "C" int sqbem_gemm_variants(int* count) {
+    if (count) *count = NVARIANTS;
+    return SQBEM_OK;
+}
+
+extern "C" int sqbem_gemm_timing(int variant, int products, int M, int N, int K, int count, float beta, int reps,
+                                 double* seconds) {
     return guarded([&] {
-        if (M < 0 || N < 0 || K <= 0 || !A || !B || !C || lda < M || ldb < K || ldc < M)
-            fail(SQBEM_ERR_ARG, "gemm_mixed: bad arguments");
-        if (M == 0 || N == 0) return;
+        if (M <= 0 || N <= 0 || K <= 0 || count <= 0 || count > MAXP || reps <= 0 || !seconds ||
+            (products != 2 && products != 3) || variant < -1 || variant >= NVARIANTS)
+            fail(SQBEM_ERR_ARG, "gemm_timing: bad arguments");
+        const long long ld = pad_ld(K);
+        const double total = (double)count * (4.0 * ((double)M + N) * ld + 4.0 * (double)M * N);
+        if (total > 16e9) fail(SQBEM_ERR_ARG, "gemm_timing: %.1f GB of operands exceed the 16 GB cap", total / 1e9);
         require_device();
-        cudaStream_t st;
-        CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        {
-            const long long ld = pad_ld(K);
-            DevBuf<float> dA((size_t)lda * K, st), dB((size_t)ldb * N, st), dC((size_t)ldc * N, st);
-            DevBuf<bf16> ah((size_t)M * ld, st), al((size_t)M * ld, st), bh((size_t)N * ld, st), bl((size_t)N * ld, st);
-            DevBuf<int> err(1, st);
-            err.zero();
-            dA.upload(A, (size_t)lda * K);
-            dB.upload(B, (size_t)ldb * N);
-            dC.upload(C, (size_t)ldc * N);
-            // A (col-major M x K) -> K-major rows; B (col-major K x N) -> K-major columns
-            split_convert(dA.get(), 1, lda, M, K, ah.get(), al.get(), ld, 1, st);
-            split_convert(dB.get(), 1, ldb, K, N, bh.get(), bl.get(), 1, ld, st);
-            TcProblem P;
-            P.M = M; P.N = N; P.K = K; P.alpha = alpha; P.beta = beta;
-            P.C = dC.get(); P.c_rs = 1; P.c_cs = ldc;
-            TcOperands o;
-            o.A = {ah.get(), al.get(), M, K, ld};
-            o.B = {bh.get(), bl.get(), N, K, ld};
-            tc_gemm({P}, {o}, err.get(), nullptr, st);
-            int h_err = 0;
-            err.download(&h_err, 1);
-            dC.download(C, (size_t)ldc * N);
-            CUDA_CHECK(cudaStreamSynchronize(st));
-            if (h_err) fail(SQBEM_ERR_TIMEOUT, "gemm_mixed: a bounded wait in the tensor-core GEMM expired");
+        CallStream cs;
+        const cudaStream_t st = cs.s;
+        std::vector<DevBuf<bf16>> planes;
+        std::vector<DevBuf<float>> cs_(count);
+        std::vector<TcProblem> P(count);
+        std::vector<TcOperands> O(count);
+        for (int q = 0; q < count; ++q) {
+            for (int w = 0; w < 4; ++w) {
+                const size_t n = (size_t)(w < 2 ? M : N) * ld;
+                planes.emplace_back(n, st);
+                LAUNCH(fill_planes_kernel, ceil_div((long long)n, 256), 256, 0, st, planes.back().get(), n,
+                       0x9e3779b9u * (unsigned)(4 * q + w + 1));
+            }
+            cs_[q].alloc((size_t)M * N, st);
+            cs_[q].zero();
+            TcProblem& p = P[q];
+            p.M = M; p.N = N; p.K = K; p.alpha = 1.f; p.beta = beta;
+            p.C = cs_[q].get(); p.c_rs = 1; p.c_cs = M;
+            p.products = products;
+            const size_t b = planes.size() - 4;
+            O[q].A = {planes[b].get(), planes[b + 1].get(), M, K, ld};
+            O[q].B = {planes[b + 2].get(), planes[b + 3].get(), N, K, ld};
         }
-        cudaStreamDestroy(st);
+        DevBuf<int> err(1, st);
+        err.zero();
+        tc_gemm(P, O, err.get(), nullptr, st, variant);  // warm-up
+        cudaEvent_t e0, e1;
+        CUDA_CHECK(cudaEventCreate(&e0));
+        CUDA_CHECK(cudaEventCreate(&e1));
+        CUDA_CHECK(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) tc_gemm(P, O, err.get(), nullptr, st, variant);
+        CUDA_CHECK(cudaEventRecord(e1, st));
+        CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int h_err = 0;
+        err.download(&h_err, 1);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (h_err) fail(SQBEM_ERR_TIMEOUT, "gemm_timing: a bounded wait in the tensor-core GEMM expired");
+        *seconds = ms * 1e-3 / reps;
+    });
+}
+
+extern "C" int sqbem_test_gemm_stall(int calls) {
+    return guarded([&] {
+        if (calls < 0) fail(SQBEM_ERR_ARG, "test_gemm_stall: negative count");
+        g_test_stalls.store(calls);
     });
 }

@@ -44,6 +44,7 @@ struct TcProblem {
     int check_unit = 0;    // flag |C| > 1 into the certificate word (LU multipliers)
     int tiles_n = 0;       // filled by the launcher
     int tile_start = 0;    // filled by the launcher
+    int products = 3;      // 3: hi*hi + hi*lo + lo*hi; 2: hi*hi + hi*lo (A rounded to BF16)
 };
 
 struct TcOperands {
@@ -52,9 +53,19 @@ struct TcOperands {
 
 // Launch all problems as one persistent grouped GEMM on stream st.
 // err (device int) receives 1 if a bounded wait timed out; flag (device int,
-// may be null) receives bit 0 if a check_unit problem saw |C| > 1.
+// may be null) receives bit 0 if a check_unit problem saw |C| > 1.  variant:
+// the kernel's tile variant (tc_gemm_variants()), or -1 for the one the tuning
+// table gives for the problems' shape class.
 void tc_gemm(const std::vector<TcProblem>& probs, const std::vector<TcOperands>& ops, int* err, int* flag,
-             cudaStream_t st);
+             cudaStream_t st, int variant = -1);
+
+// Tile variants of the GEMM kernel: count, and the tile width (N) and pipeline
+// depth of one.
+int tc_gemm_variants();
+void tc_gemm_variant_info(int variant, int* bn, int* stages);
+// The variant the tuning table gives for launches whose largest K and N are
+// kmax and nmax.
+int tc_gemm_choose(int kmax, int nmax);
 
 // Convert an FP32 matrix (element (r, c) at src[r * s_rs + c * s_cs]) into split
 // BF16 planes with element (r, c) at dst[r * d_rs + c * d_cs].

@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "concurrent.cuh"
 #include "solver.cuh"
+#include "tube_cache.cuh"
 
 using namespace sqbem;
 
@@ -58,16 +59,19 @@ struct Modes {
 // U, Omega of the B1 = 1 and B2 = 1 modes for many swimmers around one tube.
 class Evaluator {
 public:
+    // the tube comes from the cache of factored tubes (tube_cache.cu): a call
+    // with the tube of an earlier call reuses its factor
     Evaluator(const sqbem_traj_params& P, int precision) : prec_(precision) {
         a_ = 1.0;
         R_ = a_ / P.a_over_R;
-        tube_ = std::make_unique<sqbem_tube>();
-        tube_->build(R_, P.L_over_R * R_, a_, P.n_theta, 4, 1.0, precision);
+        tube_ = cached_tube(R_, P.L_over_R * R_, a_, P.n_theta, 4, 1.0, precision);
         sph0_ = bem::icosphere(a_, P.sphere_level);
     }
+    // work on st_ that reads the shared tube ends before the reference is dropped
+    ~Evaluator() { cudaStreamSynchronize(st_); }
     double R() const { return R_; }
     double a() const { return a_; }
-    cudaStream_t stream() const { return tube_->st; }
+    cudaStream_t stream() const { return st_; }
 
     // One group of swimmers built and solved for the B1 and B2 slip modes.  With
     // keep, the full solutions stay available: mixed, x = [f_t; f_s; w] per mode
@@ -78,7 +82,7 @@ public:
         std::vector<Modes> modes;
         std::vector<DevBuf<double>> dx;          // mixed
         std::vector<std::vector<double>> ft, fs; // FP64: 2 x 3 Nt, 2 x 3 Ns
-        std::vector<std::array<double, 3>> centre;
+        std::vector<std::array<double, 3>> centre, e;
     };
 
     void solve_group(const std::vector<State>& ys, size_t c0, size_t G, bool keep, Group& gr, cudaStream_t st) {
@@ -86,6 +90,7 @@ public:
         gr.slips.resize(G);
         gr.modes.resize(G);
         gr.centre.resize(G);
+        gr.e.resize(G);
         for (size_t g = 0; g < G; ++g) {
             const State& y = ys[c0 + g];
             const double c[3] = {y[0], y[1], 0.0};
@@ -102,9 +107,12 @@ public:
             } else {
                 gr.sw[g]->build(tube_.get(), S.P(), V.data(), c, 1.0, prec_);
             }
-            gr.slips[g] = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 1, 0);
-            const auto u2 = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 0, 1);
-            gr.slips[g].insert(gr.slips[g].end(), u2.begin(), u2.end());
+            gr.e[g] = {ev[0], ev[1], ev[2]};
+            if (prec_ != SQBEM_MIXED || keep) {  // host copies: the FP64 API and the field's surface velocity
+                gr.slips[g] = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 1, 0);
+                const auto u2 = squirmer_slip_host(gr.sw[g]->host_panels, c, ev, 0, 1);
+                gr.slips[g].insert(gr.slips[g].end(), u2.begin(), u2.end());
+            }
         }
         if (prec_ == SQBEM_MIXED) {
             std::vector<sqbem_swimmer*> sp;
@@ -113,33 +121,47 @@ public:
             flags.zero();
             MixedCtx cx{st, flags.get(), flags.get() + 1};
             mixed_build_swimmers(sp, cx);
+            // the slip modes on the device (slip_modes_group), solved in place
             std::vector<DevBuf<double>> din(G);
             gr.dx.clear();
             gr.dx.resize(G);
             std::vector<const double*> ip;
             std::vector<double*> xp;
+            std::vector<SlipJob> sj;
             for (size_t g = 0; g < G; ++g) {
-                din[g].alloc(gr.slips[g].size(), st);
-                din[g].upload(gr.slips[g].data(), gr.slips[g].size());
+                din[g].alloc((size_t)6 * sp[g]->Ns, st);
+                SlipJob j;
+                j.rec = sp[g]->panels.rec.get();
+                j.Ns = sp[g]->Ns;
+                for (int q = 0; q < 3; ++q) {
+                    j.xc[q] = gr.centre[g][q];
+                    j.e[q] = gr.e[g][q];
+                }
+                j.out = din[g].get();
+                sj.push_back(j);
                 gr.dx[g].alloc((size_t)(sp[g]->mx.nt + sp[g]->mx.nc) * 2, st);
                 ip.push_back(din[g].get());
                 xp.push_back(gr.dx[g].get());
             }
+            slip_modes_group(sj, st);
             int it = 0;
             double res = 0;
             mixed_solve(sp, false, ip, 2, xp, cx, &it, &res);
+            std::vector<double> w(12 * G);
             for (size_t g = 0; g < G; ++g) {
                 const MixedSwimmer& M = sp[g]->mx;
                 const size_t ld = (size_t)M.nt + M.nc;
-                std::vector<double> w(12);
                 for (int k = 0; k < 2; ++k)
-                    CUDA_CHECK(cudaMemcpyAsync(w.data() + 6 * k, gr.dx[g].get() + k * ld + M.nt + M.ns,
+                    CUDA_CHECK(cudaMemcpyAsync(w.data() + 12 * g + 6 * k, gr.dx[g].get() + k * ld + M.nt + M.ns,
                                                6 * sizeof(double), cudaMemcpyDeviceToHost, st));
                 count_d2h(12 * sizeof(double));
-                CUDA_CHECK(cudaStreamSynchronize(st));
+            }
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            for (size_t g = 0; g < G; ++g) {
+                const double* wg = w.data() + 12 * g;
                 Modes& m = gr.modes[g];
                 for (int q = 0; q < 3; ++q) {
-                    m.U1[q] = w[q]; m.O1[q] = w[3 + q]; m.U2[q] = w[6 + q]; m.O2[q] = w[9 + q];
+                    m.U1[q] = wg[q]; m.O1[q] = wg[3 + q]; m.U2[q] = wg[6 + q]; m.O2[q] = wg[9 + q];
                 }
             }
             if (!keep) gr.dx.clear();
@@ -179,7 +201,7 @@ public:
         const size_t ntask = (ys.size() + TRAJ_GROUP - 1) / TRAJ_GROUP;
         std::vector<double> bytes;
         for (size_t k = 0; k < ntask; ++k) bytes.push_back(group_bytes(std::min<size_t>(TRAJ_GROUP, ys.size() - k * TRAJ_GROUP)));
-        run_concurrent(ntask, bytes, tube_->st, [&](size_t k, cudaStream_t st) {
+        run_concurrent(ntask, bytes, st_, [&](size_t k, cudaStream_t st) {
             const size_t c0 = k * TRAJ_GROUP, G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
             Group gr;
             solve_group(ys, c0, G, false, gr, st);
@@ -196,7 +218,8 @@ public:
 private:
     int prec_;
     double a_ = 1, R_ = 1;
-    std::unique_ptr<sqbem_tube> tube_;
+    std::shared_ptr<const sqbem_tube> tube_;
+    Stream st_;  // this evaluation's own stream (the cached tube's is not used)
     bem::Mesh sph0_;
     std::atomic<long long> evals_{0};
 };
@@ -208,7 +231,7 @@ void Evaluator::fields(const std::vector<State>& ys, const double* alpha, const 
     const size_t ntask = (ys.size() + TRAJ_GROUP - 1) / TRAJ_GROUP;
     std::vector<double> bytes;
     for (size_t k = 0; k < ntask; ++k) bytes.push_back(group_bytes(std::min<size_t>(TRAJ_GROUP, ys.size() - k * TRAJ_GROUP)));
-    run_concurrent(ntask, bytes, tube_->st, [&](size_t task, cudaStream_t st) {
+    run_concurrent(ntask, bytes, st_, [&](size_t task, cudaStream_t st) {
         const size_t c0 = task * TRAJ_GROUP, G = std::min<size_t>(TRAJ_GROUP, ys.size() - c0);
         Group gr;
         solve_group(ys, c0, G, true, gr, st);

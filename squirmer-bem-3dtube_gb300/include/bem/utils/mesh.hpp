@@ -9,8 +9,8 @@
 //   * tags WALL 0, INLET 1, OUTLET 2, SPHERE 10 (mesh.hpp:45);
 //   * node order, triangle order and the floating-point operation order are the
 //     reference's, so every coordinate, normal, centroid, area and h is
-//     bit-identical (tests/test_mesh.py checks this against fixtures written by
-//     the reference).
+//     bit-identical (tests/test_abi.py::test_meshes_bitwise_match_reference
+//     checks this against fixtures written by the reference).
 #pragma once
 #include <algorithm>
 #include <array>

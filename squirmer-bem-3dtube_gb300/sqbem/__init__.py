@@ -43,6 +43,9 @@ SIGNATURES = {
     "sqbem_last_error": (ctypes.c_char_p, []),
     "sqbem_version": (ctypes.c_char_p, []),
     "sqbem_launch_count": (ctypes.c_longlong, []),
+    "sqbem_set_limits": (_c_i, [ctypes.c_longlong, _c_i]),
+    "sqbem_test_gemm_stall": (_c_i, [_c_i]),
+    "sqbem_pipe_rates": (_c_i, [_D, _D]),
     "sqbem_tube_mesh": (_c_i, [_c_d, _D, _c_i, _c_i, _c_i, _D, _I, _c_i, _I]),
     "sqbem_swimmer_tube_mesh": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _D, _I, _c_i, _I]),
     "sqbem_uniform_z": (_c_i, [_c_d, _c_d, _c_i, _D]),
@@ -74,28 +77,42 @@ SIGNATURES = {
     "sqbem_kernel_stats_classes": (_c_i, [ctypes.c_char_p, _c_i]),
     "sqbem_trim_pool": (_c_i, []),
     "sqbem_kinematics_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
+    "sqbem_kinematics_batch_tractions": (_c_i, [_c_i, _VP, _c_i, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), _D]),
     "sqbem_adjoint_batch": (_c_i, [_c_i, _VP, _c_i, _D, _D]),
     "sqbem_trajectory_defaults": (_c_i, [_VP]),
+    "sqbem_tube_cache_stats": (_c_i, [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _I]),
+    "sqbem_tube_cache_clear": (_c_i, []),
     "sqbem_run_trajectory": (_c_i, [_VP, ctypes.c_char_p, _c_i, _c_i, ctypes.c_char_p, _c_i]),
     "sqbem_trajectory_ensemble": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _D, _D, _D, _I, _D]),
     "sqbem_ensemble_field": (_c_i, [_c_i, _D, _D, _VP, _c_i, _c_i, _c_i, _c_d, _c_i, _D, _D]),
     "sqbem_gemm_mixed": (_c_i, [_c_i, _c_i, _c_i, ctypes.c_float, ctypes.POINTER(ctypes.c_float), _c_i,
                                 ctypes.POINTER(ctypes.c_float), _c_i, ctypes.c_float,
                                 ctypes.POINTER(ctypes.c_float), _c_i]),
+    "sqbem_gemm_mixed_ex": (_c_i, [_c_i, _c_i, _c_i, _c_i, _c_i, ctypes.c_float, ctypes.POINTER(ctypes.c_float), _c_i,
+                                   ctypes.POINTER(ctypes.c_float), _c_i, ctypes.c_float,
+                                   ctypes.POINTER(ctypes.c_float), _c_i]),
+    "sqbem_gemm_variants": (_c_i, [_I]),
+    "sqbem_gemm_timing": (_c_i, [_c_i, _c_i, _c_i, _c_i, _c_i, _c_i, ctypes.c_float, _c_i, _D]),
 }
 
 
-def gemm_mixed(A, B, C=None, alpha=1.0, beta=0.0):
+def gemm_mixed(A, B, C=None, alpha=1.0, beta=0.0, variant=-1, products=3):
     """linalg.hpp:42-48 gemm on the tensor cores, split-BF16 operands: returns
-    alpha A B + beta C as FP32."""
+    alpha A B + beta C as FP32.  variant: the kernel's tile variant (-1: the
+    tuning table's choice); products: 3 (hi*hi + hi*lo + lo*hi) or 2 (A rounded
+    to BF16)."""
     A = np.asfortranarray(np.asarray(A, dtype=np.float32))
     B = np.asfortranarray(np.asarray(B, dtype=np.float32))
     M, K = A.shape
     N = B.shape[1]
     Cm = np.asfortranarray(np.zeros((M, N), np.float32) if C is None else np.asarray(C, dtype=np.float32).copy())
     fp = ctypes.POINTER(ctypes.c_float)
-    _check(lib().sqbem_gemm_mixed(M, N, K, alpha, A.ctypes.data_as(fp), M, B.ctypes.data_as(fp), K, beta,
-                                  Cm.ctypes.data_as(fp), M))
+    if variant == -1 and products == 3:
+        _check(lib().sqbem_gemm_mixed(M, N, K, alpha, A.ctypes.data_as(fp), M, B.ctypes.data_as(fp), K, beta,
+                                      Cm.ctypes.data_as(fp), M))
+    else:
+        _check(lib().sqbem_gemm_mixed_ex(variant, products, M, N, K, alpha, A.ctypes.data_as(fp), M,
+                                         B.ctypes.data_as(fp), K, beta, Cm.ctypes.data_as(fp), M))
     return Cm
 
 
@@ -263,16 +280,61 @@ def _instances(instances):
     return arr
 
 
-def kinematics_batch(instances, precision=MIXED):
+def kinematics_batch(instances, precision=MIXED, tractions=False):
     """sqbem_kinematics_batch: instances = list of dicts with a_over_R, beta,
     L_over_R, e, n_theta, n_r, sphere_level, towed.  Returns (results
-    (n x RESULT_STRIDE), device seconds)."""
+    (n x RESULT_STRIDE), device seconds); with tractions=True
+    (sqbem_kinematics_batch_tractions) also the lists f_sphere and f_tube of
+    (2, N, 3) arrays per instance (slip modes B1 = 1 and B2 = 1)."""
     n = len(instances)
     arr = _instances(instances)
     res = np.zeros((n, RESULT_STRIDE))
     secs = ctypes.c_double(0)
-    _check(lib().sqbem_kinematics_batch(n, ctypes.cast(arr, _VP), precision, _dp(res), ctypes.byref(secs)))
-    return res, secs.value
+    if not tractions:
+        _check(lib().sqbem_kinematics_batch(n, ctypes.cast(arr, _VP), precision, _dp(res), ctypes.byref(secs)))
+        return res, secs.value
+    fs = [np.zeros((2, 20 * 4 ** int(d["sphere_level"]), 3)) for d in instances]
+    ft = [np.zeros((2, _tube_panels(d), 3)) for d in instances]
+    ps = (_D * max(n, 1))(*[_dp(a) for a in fs])
+    pt = (_D * max(n, 1))(*[_dp(a) for a in ft])
+    _check(lib().sqbem_kinematics_batch_tractions(n, ctypes.cast(arr, _VP), precision, _dp(res), ps, pt,
+                                                  ctypes.byref(secs)))
+    return res, secs.value, fs, ft
+
+
+def _tube_panels(d):
+    """panel count of an instance's tube (0 for the unbounded fluid)"""
+    if d["a_over_R"] <= 0:
+        return 0
+    R = 1.0 / d["a_over_R"]
+    P = ctypes.c_int(0)
+    _check(lib().sqbem_swimmer_tube_mesh(R, d.get("L_over_R", 4.0) * R, 1.0, int(d.get("n_theta", 24)),
+                                         int(d.get("n_r", 4)), None, None, 0, ctypes.byref(P)))
+    return P.value
+
+
+def tube_cache_stats():
+    """(tubes built, cache hits, entries held) of the trajectory calls' tube cache"""
+    b, h, e = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_int(0)
+    _check(lib().sqbem_tube_cache_stats(ctypes.byref(b), ctypes.byref(h), ctypes.byref(e)))
+    return b.value, h.value, e.value
+
+
+def tube_cache_clear():
+    _check(lib().sqbem_tube_cache_clear())
+
+
+def set_limits(gemm_wait_cycles=-1, refine_max_iterations=-1):
+    """sqbem_set_limits: bounded-wait length of the tensor-core GEMM (SM cycles)
+    and the refinement cap; -1 restores a default."""
+    _check(lib().sqbem_set_limits(int(gemm_wait_cycles), int(refine_max_iterations)))
+
+
+def pipe_rates():
+    """(FP64, FP32) FMA throughput of this GPU in TFLOP/s, measured now."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    _check(lib().sqbem_pipe_rates(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def adjoint_batch(instances, precision=FP64):

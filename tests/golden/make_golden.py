@@ -18,6 +18,11 @@ Cases (all FP64, 17 significant digits):
   c2          a/R = 0.3, beta = 0, level 3, n_theta = 24 (full kinematics size)
   c2_l2       level-2 cases at n_theta = 24 (on axis, off axis, tilted)
   traj        a 6-step trajectory (3 RK4 + 3 AB4) on a small mesh (CSV, 10 digits)
+  ref_outputs the reference's own stored results, copied as text: the input files
+              inputs/{duct_flow,squirmer_kinematics,squirmer_field}.in and the
+              CSVs outputs/duct_flow/{flow_rate,profile,panels}.csv and
+              outputs/reference/squirmer/{axis,offaxis,field,blake,reciprocal}.csv
+              (10 digits; written by the reference's own programs)
 """
 import json
 import os
@@ -27,10 +32,38 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DUMPER = os.path.join(HERE, "..", "..", "oracle", "_ref", "ref_dump")
-CASES = ["mesh", "panel", "swim_small", "duct_small", "duct_c1", "c2", "c2_l2", "traj"]
+CASES = ["mesh", "panel", "swim_small", "duct_small", "duct_c1", "c2", "c2_l2", "traj", "ref_outputs"]
+STORED = ["inputs/duct_flow.in", "inputs/squirmer_kinematics.in", "inputs/squirmer_field.in",
+          "outputs/duct_flow/flow_rate.csv", "outputs/duct_flow/profile.csv", "outputs/duct_flow/panels.csv",
+          "outputs/reference/squirmer/axis.csv", "outputs/reference/squirmer/offaxis.csv",
+          "outputs/reference/squirmer/field.csv", "outputs/reference/squirmer/blake.csv",
+          "outputs/reference/squirmer/reciprocal.csv"]
+
+
+def reference_dir():
+    """the reference checkout that oracle/Makefile names"""
+    ref = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "..", "..", "oracle"), "refdir"],
+                         capture_output=True, text=True).stdout.strip()
+    if not ref:
+        raise SystemExit("reference checkout not found (see oracle/Makefile)")
+    return ref
+
+
+def stored_outputs():
+    ref = reference_dir()
+    obj = {}
+    for rel in STORED:
+        with open(os.path.join(ref, rel)) as f:
+            obj[rel] = f.read()
+    return obj
 
 
 def run(case):
+    if case == "ref_outputs":
+        obj = stored_outputs()
+        with open(os.path.join(HERE, case + ".json"), "w") as f:
+            json.dump(obj, f, indent=0)
+        return obj
     with tempfile.TemporaryDirectory() as tmp:
         out = subprocess.run([DUMPER, case, tmp], check=True, capture_output=True, text=True,
                              env=dict(os.environ, OPENBLAS_NUM_THREADS="8"))

@@ -10,12 +10,14 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.path.join(os.sep, "root", "reference")
+# the reference checkout, where oracle/Makefile finds one ("" otherwise)
+REF = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "refdir"], capture_output=True,
+                     text=True).stdout.strip()
 LIBDIR = os.path.join(ROOT, "squirmer-bem-3dtube_gb300", "lib")
 INC = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "squirmer-bem-3dtube_gb300", "include", "bem")]
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference sources not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "src")), reason="reference sources not present")
 @pytest.mark.parametrize("src", ["src/main.cpp", "tests/test_duct_flow.cpp", "tests/test_squirmer.cpp",
                                  "tests/test_trajectory.cpp"])
 def test_reference_program_builds_against_dropin(tmp_path, src):

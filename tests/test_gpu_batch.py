@@ -16,6 +16,11 @@ def uo_err(a, b):
     return np.linalg.norm(a[:, :12] - b[:, :12], axis=1) / np.linalg.norm(b[:, :12], axis=1)
 
 
+def rel(a, b):
+    """max-abs relative error of a traction field"""
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(np.asarray(b))))
+
+
 def test_batch_small_mixed_vs_fp64():
     rng = np.random.default_rng(5)
     insts = []
@@ -46,6 +51,47 @@ def test_batch_fp64_matches_single_solves():
     r, _ = sqbem.kinematics_batch([inst], sqbem.FP64)
     ref = np.concatenate([g["B1"]["U"], g["B1"]["Om"], g["B2"]["U"], g["B2"]["Om"]])
     assert np.max(np.abs(r[0, :12] - ref)) < 1e-10 * np.max(np.abs(ref))
+
+
+def test_batch_tractions_fp64_vs_reference():
+    """sqbem_kinematics_batch_tractions: the f_sphere and f_tube of both slip
+    modes (SwimmerSolution, swimmer.hpp:78-81) against the reference's dump"""
+    g = golden("c2_l2")["l2_off"]
+    inst = dict(a_over_R=g["a_over_R"], beta=g["beta"], L_over_R=4.0, e=tuple(g["e"]), n_theta=24, n_r=4,
+                sphere_level=2, towed=0)
+    r, _, fs, ft = sqbem.kinematics_batch([inst], sqbem.FP64, tractions=True)
+    r0, _ = sqbem.kinematics_batch([inst], sqbem.FP64)
+    np.testing.assert_array_equal(r[0, :12], r0[0, :12])
+    for m, mode in enumerate(("B1", "B2")):
+        assert rel(fs[0][m].reshape(-1), g[mode]["f_sphere"]) < 1e-10
+        assert rel(ft[0][m].reshape(-1), g[mode]["f_tube"]) < 1e-10
+    rm, _, fsm, ftm = sqbem.kinematics_batch([inst], sqbem.MIXED, tractions=True)
+    for m, mode in enumerate(("B1", "B2")):
+        assert rel(fsm[0][m].reshape(-1), g[mode]["f_sphere"]) < 1e-5
+        assert rel(ftm[0][m].reshape(-1), g[mode]["f_tube"]) < 1e-5
+
+
+@pytest.mark.slow
+def test_batch_whole_sweep_mixed_vs_fp64():
+    """every one of the 128 instances the headline benchmark times, as the
+    squirmer B2/B1 = alpha each instance draws: U within 1e-6 of the FP64 path,
+    Omega within 1e-6 in units of U/a (Omega vanishes on the axis), the stacked
+    (U, Omega) of both slip modes within 1e-6; the sphere and wall tractions
+    within 5e-5 max-abs relative (measured worst 1.3e-5, on the wall of a
+    near-wall instance: the FP32 storage of the assembled blocks sets it)"""
+    insts = workloads.sweep()
+    rmx, _, fsm, ftm = sqbem.kinematics_batch(insts, sqbem.MIXED, tractions=True)
+    r64, _, fs64, ft64 = sqbem.kinematics_batch(insts, sqbem.FP64, tractions=True)
+    err = uo_err(rmx, r64)
+    assert np.all(err < 1e-6), (float(err.max()), int(err.argmax()))
+    for k, d in enumerate(insts):
+        al = d["alpha"]
+        U, U64 = rmx[k, 0:3] + al * rmx[k, 6:9], r64[k, 0:3] + al * r64[k, 6:9]
+        W, W64 = rmx[k, 3:6] + al * rmx[k, 9:12], r64[k, 3:6] + al * r64[k, 9:12]
+        assert np.linalg.norm(U - U64) < 1e-6 * np.linalg.norm(U64), k
+        assert np.linalg.norm(W - W64) < 1e-6 * max(np.linalg.norm(W64), np.linalg.norm(U64)), k
+        for A, B in ((fsm[k], fs64[k]), (ftm[k], ft64[k])):
+            assert rel(A[0] + al * A[1], B[0] + al * B[1]) < 5e-5, k
 
 
 def test_batch_sweep_instances_mixed_vs_fp64():

@@ -135,6 +135,47 @@ def test_ensemble_mixed_vs_fp64_rk4():
     assert np.max(np.abs(Umx - U64)) < 1e-6 * np.max(np.abs(U64))
 
 
+def test_ensemble_mixed_vs_fp64_config5_mesh():
+    """the trajectory-ensemble workload's own mesh (a/R = 0.3, n_theta = 24,
+    level 2, dt = 0.05): 8 of its swimmers, 4 RK4 steps, mixed against FP64"""
+    from sqbem import workloads
+    w = workloads.ensemble()[:8]
+    P = sqbem.TrajParams(a_over_R=w[0]["a_over_R"], dt=w[0]["dt"], n_theta=w[0]["n_theta"],
+                         sphere_level=w[0]["sphere_level"], L_over_R=w[0]["L_over_R"])
+    R = 1.0 / P.a_over_R
+    y0 = np.array([[d["beta0"] * (R - 1.0), 0.0, 0.0, *d["e"]] for d in w])
+    alpha = np.array([d["alpha"] for d in w])
+    s64, U64, O64, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 4, scheme=1, precision=sqbem.FP64)
+    smx, Umx, Omx, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 4, scheme=1, precision=sqbem.MIXED)
+    assert np.max(np.abs(smx - s64)) < 1e-6 * np.max(np.abs(s64))
+    for k in range(len(w)):
+        uo = np.concatenate([Umx[k].reshape(-1), Omx[k].reshape(-1)])
+        ref = np.concatenate([U64[k].reshape(-1), O64[k].reshape(-1)])
+        assert np.linalg.norm(uo - ref) < 1e-6 * np.linalg.norm(ref), k
+
+
+def test_tube_factor_shared_across_calls():
+    """two ensemble calls and a field call around the same tube assemble and
+    factor it once (the cache of factored tubes); results are unchanged"""
+    P = sqbem.TrajParams(a_over_R=0.3, dt=0.25, n_theta=9, sphere_level=1)
+    rng = np.random.default_rng(17)
+    y0 = _initial_states(P, 3, rng)
+    alpha = rng.uniform(-5, 5, 3)
+    sqbem.tube_cache_clear()
+    b0, h0, _ = sqbem.tube_cache_stats()
+    s1, U1, _, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 2, scheme=1, precision=sqbem.MIXED)
+    s2, U2, _, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 2, scheme=1, precision=sqbem.MIXED)
+    sqbem.ensemble_field(s2[:, -1, :], alpha, P, 5, 5, 7, 7.0, precision=sqbem.MIXED)
+    b1, h1, n = sqbem.tube_cache_stats()
+    assert b1 - b0 == 1 and h1 - h0 == 2 and n >= 1
+    np.testing.assert_array_equal(s1, s2)
+    np.testing.assert_array_equal(U1, U2)
+    sqbem.tube_cache_clear()
+    s3, _, _, _, _ = sqbem.trajectory_ensemble(y0, alpha, P, 2, scheme=1, precision=sqbem.MIXED)
+    assert sqbem.tube_cache_stats()[0] - b1 == 1
+    np.testing.assert_array_equal(s1, s3)
+
+
 def test_ensemble_wall_contact_freezes_member():
     P = sqbem.TrajParams(a_over_R=0.3, dt=0.5, n_theta=8, sphere_level=1, beta_stop=0.5)
     R = 1.0 / P.a_over_R
