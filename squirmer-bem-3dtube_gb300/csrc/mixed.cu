@@ -42,6 +42,7 @@ void MixedLU::alloc(int nt, cudaStream_t st) {
     LiRh.alloc(nb, st); LiRl.alloc(nb, st);
     UiRh.alloc(nb, st); UiRl.alloc(nb, st);
     UiCh.alloc(nb, st); UiCl.alloc(nb, st);
+    LiCh.alloc(nb, st); LiCl.alloc(nb, st);
 }
 
 namespace {
@@ -112,7 +113,7 @@ struct DiagJob {
     long long lda;
     float* Li;
     float* Ui;
-    bf16 *LiRh, *LiRl, *UiRh, *UiRl, *UiCh, *UiCl;
+    bf16 *LiRh, *LiRl, *UiRh, *UiRl, *UiCh, *UiCl, *LiCh, *LiCl;
 };
 
 constexpr int DIAG_THREADS = 512;
@@ -376,6 +377,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
         J.Li[r + c * N] = xl[r][c];
         J.Ui[r + c * N] = xu[r][c];
         put_split(J.UiCh, J.UiCl, (long long)c * N + r, xu[r][c]);
+        put_split(J.LiCh, J.LiCl, (long long)c * N + r, xl[r][c]);
     }
     for (int e = tid; e < N * N; e += DIAG_THREADS) {
         const int r = e / N, c = e % N;  // row-major: consecutive threads along a row
@@ -434,13 +436,57 @@ void run(std::vector<TcProblem>& P, std::vector<TcOperands>& O, const MixedCtx& 
 // tri: the right-hand side is lower triangular from column j0 on (the identity
 // of an inversion), so in the lower solve column c of X stays zero above row c
 // and only columns c < k0 + w (relative to j0: c - j0 < k0 + w) take part.
+// wide (the members carry their composed 256-block inverses; scratch: one
+// 256 x ncols column-major split plane pair per member): the recursion splits at
+// multiples of 256 and its leaves are 256 rows wide -- one conversion and one
+// GEMM with K = 256 instead of two 128-row leaves and the K = 128 update
+// between them; a trailing odd 128-block takes the 128-row leaf.
+struct WideScratch {
+    std::vector<bf16*> hi, lo;
+};
 void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool lower, int k0, int w, int j0,
-          const std::vector<int>& ncols_in, const MixedCtx& cx, bool tri = false) {
+          const std::vector<int>& ncols_in, const MixedCtx& cx, bool tri = false, const WideScratch* ws = nullptr) {
     std::vector<TcProblem> P;
     std::vector<TcOperands> O;
     std::vector<int> ncols = ncols_in;
     if (tri && lower)
         for (int& c : ncols) c = std::min(c, k0 + w);
+    constexpr int W2 = 2 * MX_NB;
+    if (ws && w == W2) {
+        // wide leaf: S = split(X rows [k0, k0 + 256)), X = inv256 * S (S is a copy: the
+        // two 128-row output tiles both read all 256 rows of it)
+        std::vector<ConvJob> cj;
+        for (size_t m = 0; m < g.size(); ++m) {
+            if (ncols[m] <= 0) continue;
+            const Target& t = T[m];
+            cj.push_back({t.X + k0 + (long long)j0 * t.ldx, 1, t.ldx, W2, ncols[m], ws->hi[m], ws->lo[m], 1, W2});
+        }
+        convert_group(cj, cx.st);
+        const long long qo = (long long)(k0 / W2) * W2 * W2;
+        for (size_t m = 0; m < g.size(); ++m) {
+            if (ncols[m] <= 0) continue;
+            MixedLU& L = *g[m];
+            const Target& t = T[m];
+            TcProblem p;
+            p.M = W2; p.N = ncols[m]; p.K = W2;
+            p.alpha = 1.f; p.beta = 0.f;
+            p.C = t.X + k0 + (long long)j0 * t.ldx; p.c_rs = 1; p.c_cs = t.ldx;
+            p.O_hi = t.Ch + k0 + (long long)j0 * t.ldc; p.O_lo = t.Cl + k0 + (long long)j0 * t.ldc;
+            p.o_rs = 1; p.o_cs = t.ldc;
+            if (t.Rh && !(tri && lower)) {
+                p.P_hi = t.Rh + (long long)k0 * t.ldr + j0; p.P_lo = t.Rl + (long long)k0 * t.ldr + j0;
+                p.p_rs = t.ldr; p.p_cs = 1;
+            }
+            TcOperands o;
+            o.A = lower ? SplitMat{L.L2h.get() + qo, L.L2l.get() + qo, W2, W2, W2}
+                        : SplitMat{L.U2h.get() + qo, L.U2l.get() + qo, W2, W2, W2};
+            o.B = SplitMat{ws->hi[m], ws->lo[m], ncols[m], W2, W2};
+            P.push_back(p);
+            O.push_back(o);
+        }
+        run(P, O, cx);
+        return;
+    }
     if (w == MX_NB) {
         // leaf: B -> split (column-major), X = inv_b * B, keep the split copies equal to X
         std::vector<ConvJob> cj;
@@ -479,11 +525,11 @@ void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool low
         run(P, O, cx);
         return;
     }
-    const int w1 = std::max(MX_NB, (w / MX_NB / 2) * MX_NB), w2 = w - w1;
+    const int w1 = ws ? std::max(W2, (w / W2 / 2) * W2) : std::max(MX_NB, (w / MX_NB / 2) * MX_NB), w2 = w - w1;
     // lower: first half solves, then updates the second; upper: the reverse
     const int ka = lower ? k0 : k0 + w1, wa = lower ? w1 : w2;  // solved first
     const int kb = lower ? k0 + w1 : k0, wb = lower ? w2 : w1;  // updated, solved second
-    trsm(g, T, lower, ka, wa, j0, ncols, cx, tri);
+    trsm(g, T, lower, ka, wa, j0, ncols, cx, tri, ws);
     for (size_t m = 0; m < g.size(); ++m) {
         const int nc = tri && lower ? std::min(ncols[m], ka + wa) : ncols[m];
         if (nc <= 0) continue;
@@ -500,7 +546,7 @@ void trsm(const std::vector<MixedLU*>& g, const std::vector<Target>& T, bool low
         O.push_back(o);
     }
     run(P, O, cx);
-    trsm(g, T, lower, kb, wb, j0, ncols, cx, tri);
+    trsm(g, T, lower, kb, wb, j0, ncols, cx, tri, ws);
 }
 
 void leaf(const std::vector<MixedLU*>& g, int c0, const MixedCtx& cx) {
@@ -510,7 +556,7 @@ void leaf(const std::vector<MixedLU*>& g, int c0, const MixedCtx& cx) {
         const long long bo = (long long)b * MX_NB * MX_NB;
         dj.push_back({L->A.get() + c0 + (long long)c0 * L->n, L->n, L->Li.get() + bo, L->Ui.get() + bo,
                       L->LiRh.get() + bo, L->LiRl.get() + bo, L->UiRh.get() + bo, L->UiRl.get() + bo,
-                      L->UiCh.get() + bo, L->UiCl.get() + bo});
+                      L->UiCh.get() + bo, L->UiCl.get() + bo, L->LiCh.get() + bo, L->LiCl.get() + bo});
     }
     diag_group(dj, cx);
     const int n = g[0]->n, rows = n - c0 - MX_NB;
@@ -850,6 +896,122 @@ void mixed_lu_factor(const std::vector<MixedLU*>& g, const MixedCtx& cx) {
     lu_rec(g, 0, n, cx);
 }
 
+namespace {
+// The three quadrants of each composed 256-block inverse that are copies or
+// zeros: L2 = [L11i 0; . L22i], U2 = [U11i .; 0 U22i] (row-major split, ld 256);
+// the off-diagonal quadrants come from the GEMMs of compose_wide.
+struct FillJob {
+    const bf16 *lrh, *lrl, *urh, *url;  // LiR, UiR split copies of the 128-blocks (row-major)
+    bf16 *l2h, *l2l, *u2h, *u2l;
+    int nb2;
+};
+struct FillArgs {
+    FillJob j[MAXJOBS];
+};
+__global__ void compose_fill_kernel(const __grid_constant__ FillArgs args) {
+    const FillJob& J = args.j[blockIdx.y];
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    constexpr int B = MX_NB, B2 = 2 * MX_NB;
+    if (e >= (long long)J.nb2 * B2 * B2) return;
+    const int q = (int)(e / (B2 * B2)), rc = (int)(e % (B2 * B2)), r = rc / B2, c = rc % B2;
+    const long long o = (long long)q * B2 * B2 + rc;
+    const bf16 zero = __float2bfloat16_rn(0.f);
+    if (r < B && c < B) {  // block 2q
+        const long long i = (long long)(2 * q) * B * B + r * B + c;
+        J.l2h[o] = J.lrh[i]; J.l2l[o] = J.lrl[i];
+        J.u2h[o] = J.urh[i]; J.u2l[o] = J.url[i];
+    } else if (r >= B && c >= B) {  // block 2q + 1
+        const long long i = (long long)(2 * q + 1) * B * B + (r - B) * B + (c - B);
+        J.l2h[o] = J.lrh[i]; J.l2l[o] = J.lrl[i];
+        J.u2h[o] = J.urh[i]; J.u2l[o] = J.url[i];
+    } else if (r < B) {  // upper-right: zero in L2, the GEMM's in U2
+        J.l2h[o] = zero; J.l2l[o] = zero;
+    } else {  // lower-left: zero in U2, the GEMM's in L2
+        J.u2h[o] = zero; J.u2l[o] = zero;
+    }
+}
+
+// inv([L11 0; L21 L22]) = [L11i 0; -L22i L21 L11i  L22i] and
+// inv([U11 U12; 0 U22]) = [U11i -U11i U12 U22i; 0 U22i] for every pair of
+// 128-blocks: two grouped GEMM launches (T = L21 L11i and U12 U22i, then the
+// products with -L22i and -U11i) on top of the factor's split copies.
+void compose_wide(const std::vector<MixedLU*>& g, const MixedCtx& cx) {
+    const int n = g[0]->n, nb2 = n / (2 * MX_NB);
+    constexpr int B = MX_NB, B2 = 2 * MX_NB;
+    if (nb2 == 0) {
+        for (MixedLU* L : g) L->wide = true;
+        return;
+    }
+    const size_t per = (size_t)nb2 * B2 * B2, tper = (size_t)nb2 * B * B;
+    std::vector<DevBuf<bf16>> th(g.size()), tl(g.size()), uh(g.size()), ul(g.size());
+    for (size_t m0 = 0; m0 < g.size(); m0 += MAXJOBS) {
+        FillArgs a;
+        const int cnt = (int)std::min<size_t>(MAXJOBS, g.size() - m0);
+        for (int k = 0; k < cnt; ++k) {
+            MixedLU& L = *g[m0 + k];
+            L.L2h.alloc(per, cx.st); L.L2l.alloc(per, cx.st);
+            L.U2h.alloc(per, cx.st); L.U2l.alloc(per, cx.st);
+            a.j[k] = {L.LiRh.get(), L.LiRl.get(), L.UiRh.get(), L.UiRl.get(), L.L2h.get(), L.L2l.get(),
+                      L.U2h.get(), L.U2l.get(), nb2};
+        }
+        LAUNCH(compose_fill_kernel, dim3((unsigned)ceil_div((long long)per, 256), (unsigned)cnt), 256, 0, cx.st, a);
+    }
+    std::vector<TcProblem> P;
+    std::vector<TcOperands> O;
+    for (size_t m = 0; m < g.size(); ++m) {
+        MixedLU& L = *g[m];
+        th[m].alloc(tper, cx.st); tl[m].alloc(tper, cx.st);
+        uh[m].alloc(tper, cx.st); ul[m].alloc(tper, cx.st);
+        for (int q = 0; q < nb2; ++q) {
+            const int k0 = q * B2, b0 = 2 * q, b1 = 2 * q + 1;
+            const long long bo0 = (long long)b0 * B * B, bo1 = (long long)b1 * B * B, to = (long long)q * B * B;
+            TcProblem p;  // T_L = L21 L11i -> column-major split
+            p.M = B; p.N = B; p.K = B;
+            p.O_hi = th[m].get() + to; p.O_lo = tl[m].get() + to; p.o_rs = 1; p.o_cs = B;
+            TcOperands o;
+            o.A = rview(L.Rh.get(), L.Rl.get(), L.n, k0 + B, k0, B, B);
+            o.B = SplitMat{L.LiCh.get() + bo0, L.LiCl.get() + bo0, B, B, B};
+            P.push_back(p);
+            O.push_back(o);
+            TcProblem pu = p;  // T_U = U12 U22i
+            pu.O_hi = uh[m].get() + to; pu.O_lo = ul[m].get() + to;
+            TcOperands ou;
+            ou.A = rview(L.Rh.get(), L.Rl.get(), L.n, k0, k0 + B, B, B);
+            ou.B = SplitMat{L.UiCh.get() + bo1, L.UiCl.get() + bo1, B, B, B};
+            P.push_back(pu);
+            O.push_back(ou);
+        }
+    }
+    run(P, O, cx);
+    for (size_t m = 0; m < g.size(); ++m) {
+        MixedLU& L = *g[m];
+        for (int q = 0; q < nb2; ++q) {
+            const int b0 = 2 * q, b1 = 2 * q + 1;
+            const long long bo0 = (long long)b0 * B * B, bo1 = (long long)b1 * B * B, to = (long long)q * B * B;
+            const long long qo = (long long)q * B2 * B2;
+            TcProblem p;  // L2 lower-left = -L22i T_L
+            p.M = B; p.N = B; p.K = B; p.alpha = -1.f;
+            p.O_hi = L.L2h.get() + qo + (long long)B * B2; p.O_lo = L.L2l.get() + qo + (long long)B * B2;
+            p.o_rs = B2; p.o_cs = 1;
+            TcOperands o;
+            o.A = SplitMat{L.LiRh.get() + bo1, L.LiRl.get() + bo1, B, B, B};
+            o.B = SplitMat{th[m].get() + to, tl[m].get() + to, B, B, B};
+            P.push_back(p);
+            O.push_back(o);
+            TcProblem pu = p;  // U2 upper-right = -U11i T_U
+            pu.O_hi = L.U2h.get() + qo + B; pu.O_lo = L.U2l.get() + qo + B;
+            TcOperands ou;
+            ou.A = SplitMat{L.UiRh.get() + bo0, L.UiRl.get() + bo0, B, B, B};
+            ou.B = SplitMat{uh[m].get() + to, ul[m].get() + to, B, B, B};
+            P.push_back(pu);
+            O.push_back(ou);
+        }
+        L.wide = true;
+    }
+    run(P, O, cx);
+}
+}  // namespace
+
 void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs, const MixedCtx& cx,
                     bool identity_rhs) {
     if (g.empty()) return;
@@ -864,8 +1026,20 @@ void mixed_lu_solve(const std::vector<MixedLU*>& g, const std::vector<Rhs>& rhs,
     }
     if (maxc == 0) return;
     const int n = g[0]->n;
-    trsm(g, T, true, 0, n, 0, nc, cx, identity_rhs);
-    trsm(g, T, false, 0, n, 0, nc, cx);
+    bool all_wide = true;
+    for (MixedLU* L : g) all_wide = all_wide && L->wide;
+    if (!all_wide) compose_wide(g, cx);
+    // the wide leaves' conversion targets, one 256-row split slab per member
+    std::vector<DevBuf<bf16>> sh(g.size()), sl(g.size());
+    WideScratch ws;
+    for (size_t m = 0; m < g.size(); ++m) {
+        sh[m].alloc((size_t)2 * MX_NB * std::max(nc[m], 1), cx.st);
+        sl[m].alloc((size_t)2 * MX_NB * std::max(nc[m], 1), cx.st);
+        ws.hi.push_back(sh[m].get());
+        ws.lo.push_back(sl[m].get());
+    }
+    trsm(g, T, true, 0, n, 0, nc, cx, identity_rhs, &ws);
+    trsm(g, T, false, 0, n, 0, nc, cx, false, &ws);
 }
 
 }  // namespace sqbem

@@ -26,7 +26,12 @@ struct MixedLU {
     DevBuf<bf16> Rh, Rl;    // split copy, row-major (ld n): L blocks and U blocks used as the left operand
     DevBuf<bf16> Ch, Cl;    // split copy, column-major (ld n): U blocks used as the right operand
     DevBuf<float> Li, Ui;   // per diagonal block: L^{-1} and U^{-1} (128 x 128, column-major)
-    DevBuf<bf16> LiRh, LiRl, UiRh, UiRl, UiCh, UiCl;  // their split copies (row- / column-major)
+    DevBuf<bf16> LiRh, LiRl, UiRh, UiRl, UiCh, UiCl, LiCh, LiCl;  // their split copies (row- / column-major)
+    // the inverses of the factor's 256 x 256 diagonal blocks (row-major split,
+    // ld 256, one per pair of 128-blocks), composed after the factorization for
+    // the solves' 256-wide leaves
+    DevBuf<bf16> L2h, L2l, U2h, U2l;
+    bool wide = false;
     void alloc(int n_true, cudaStream_t st);
 };
 
