@@ -22,6 +22,7 @@
 #include "common.cuh"
 #include "concurrent.cuh"
 #include "solver.cuh"
+#include "sphere_share.cuh"
 
 using namespace sqbem;
 
@@ -224,7 +225,8 @@ struct PhaseClock {
 // One chunk of a group (members with equal padded tube size and sphere size),
 // everything on stream bs.
 void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_instance* inst,
-               const std::vector<Prepared>& prep, cudaStream_t bs, const Outputs& out, PhaseClock& pc) {
+               const std::vector<Prepared>& prep, cudaStream_t bs, const Outputs& out, PhaseClock& pc,
+               const std::shared_ptr<const SphereBlocks>& share) {
     double* const results = out.results;
     const size_t G = ids.size();
     DevBuf<int> flags(2, bs);
@@ -259,7 +261,7 @@ void run_chunk(const std::vector<int>& ids, int ntp_k, int ns_k, const sqbem_ins
         sws[g]->set_geometry(tubes[g].get(), P.sphere.P(), P.sphereV.data(), c, 1.0, SQBEM_MIXED);
         sp.push_back(sws[g].get());
     }
-    mixed_build_swimmers(sp, cx);
+    mixed_build_swimmers(sp, cx, share);
     pc.lap("swimmers", G, ntp_k, ns_k);
     // the B1 = 1 and B2 = 1 slip modes of every member, on the device
     std::vector<DevBuf<double>> slip(G), xs(G);
@@ -383,9 +385,18 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
     });
     std::vector<double> bytes;
     for (const Chunk& c : chunks) bytes.push_back(chunk_bytes(c.ids.size(), c.ntp, c.ns));
+    // the sphere-sphere blocks, translation invariant: assembled once per sphere
+    // size for this call from its first instance, and shared by every chunk
+    std::map<int, std::shared_ptr<const SphereBlocks>> shares;
+    for (const Chunk& c : chunks) {
+        if (shares.count(c.ns)) continue;
+        const Prepared& P = prep[c.ids[0]];
+        const double xc[3] = {P.b, 0, 0};
+        shares[c.ns] = build_sphere_blocks(make_panels(P.sphereV.data(), P.sphere.P()), xc, 1.0, bs);
+    }
     run_concurrent(chunks.size(), bytes, bs, [&](size_t k, cudaStream_t st) {
         PhaseClock pc;
-        run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, out, pc);
+        run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, out, pc, shares[chunks[k].ns]);
     });
 }
 

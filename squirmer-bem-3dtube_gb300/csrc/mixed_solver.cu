@@ -236,7 +236,8 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
 }
 
 // ---------------------------------------------------------------- swimmers
-void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx) {
+void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx,
+                          const std::shared_ptr<const SphereBlocks>& share) {
     if (sw.empty()) return;
     const size_t G = sw.size();
     const bool bounded = sw[0]->tube != nullptr;
@@ -252,10 +253,19 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         M.nc = M.ns + 6;
         M.nsp = pad128(M.ns);
         const int ns = M.ns, nt = M.nt;
-        M.E.alloc((size_t)ns * ns, cx.st);
+        const bool shared = share && share->matches(s->host_panels, s->xc, s->mu);
+        M.sphere = shared ? share : nullptr;
+        if (!shared) M.E.alloc((size_t)ns * ns, cx.st);
         M.AuBs.alloc((size_t)ns * ns, cx.st);
         DevBuf<double> rsum((size_t)ns * 3, cx.st);
-        rsum.zero();
+        if (shared) {  // the sphere's own row sums first, the tube's added below
+            CUDA_CHECK(cudaMemcpyAsync(rsum.get(), share->rsum.get(), sizeof(double) * ns * 3,
+                                       cudaMemcpyDeviceToDevice, cx.st));
+            CUDA_CHECK(cudaMemcpyAsync(M.AuBs.get(), share->D.get(), sizeof(float) * (size_t)ns * ns,
+                                       cudaMemcpyDeviceToDevice, cx.st));
+        } else {
+            rsum.zero();
+        }
         if (bounded) {
             M.B.alloc((size_t)nt * ns, cx.st);
             M.AuBt.alloc((size_t)nt * ns, cx.st);
@@ -267,11 +277,13 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             assemble_block(j2, cap_pairs(Ns, Nt), cx.st, true);
             add_rowsums<float>(Dt.get(), 1, ns, ns, Nt, rsum.get(), cx.st);
         }
-        auto j3 = fjob(s->panels, s->panels, true, s->mu, M.E.get(), ns, M.AuBs.get(), ns);
-        assemble_block(j3, cap_pairs(Ns, Ns), cx.st, true);
-        add_rowsums<float>(M.AuBs.get(), 1, ns, ns, Ns, rsum.get(), cx.st);
+        if (!shared) {
+            auto j3 = fjob(s->panels, s->panels, true, s->mu, M.E.get(), ns, M.AuBs.get(), ns);
+            assemble_block(j3, cap_pairs(Ns, Ns), cx.st, true);
+            add_rowsums<float>(M.AuBs.get(), 1, ns, ns, Ns, rsum.get(), cx.st);
+            deflate<float>(M.E.get(), 1, ns, s->panels, s->mu, cx.st);
+        }
         diag_complete<float>(M.AuBs.get(), 1, ns, Ns, rsum.get(), bounded ? 0.0 : 1.0, nullptr, cx.st);
-        deflate<float>(M.E.get(), 1, ns, s->panels, s->mu, cx.st);
         // rigid-body map, C = A_u K (accumulated in FP64, stored FP32)   (swimmer.hpp:222-234)
         const auto Kh = rigid_map(s->host_panels, s->xc);
         M.K.alloc(Kh.size(), cx.st);
@@ -304,7 +316,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         MixedSwimmer& M = sw[k]->mx;
         glu[k].alloc(M.ns, cx.st);
         glu[k].A.zero();
-        cj.push_back(cp32_32(M.E.get(), M.ns, glu[k].A.get(), M.nsp, M.ns, M.ns));
+        cj.push_back(cp32_32(M.e(), M.ns, glu[k].A.get(), M.nsp, M.ns, M.ns));
         pad_identity(glu[k].A.get(), M.nsp, M.ns, M.nsp, cx.st);
         Gc[k].alloc((size_t)M.ns * 6, cx.st);
         cj.push_back(cp32_32(M.Cs.get(), M.ns, Gc[k].get(), M.ns, M.ns, 6));
@@ -524,7 +536,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
                         mj.push_back(mv64(M.F.get(), 6, 6, M.ns, xsp, ldx, r, W[k].rc.get(), 6, -1.0, 0.0));
                 } else if (round == 1) {
                     if (bounded) mj.push_back(mv32(M.B.get(), M.nt, M.nt, M.ns, xsp, ldx, r, rt, M.nt, -1.0, 1.0));
-                    mj.push_back(mv32(M.E.get(), M.ns, M.ns, M.ns, xsp, ldx, r, rs, M.ns, -1.0, 1.0));
+                    mj.push_back(mv32(M.e(), M.ns, M.ns, M.ns, xsp, ldx, r, rs, M.ns, -1.0, 1.0));
                 } else {
                     if (bounded) mj.push_back(mv32(M.Ct.get(), M.nt, M.nt, 6, xw, ldx, r, rt, M.nt, -1.0, 1.0));
                     mj.push_back(mv32(M.Cs.get(), M.ns, M.ns, 6, xw, ldx, r, rs, M.ns, -1.0, 1.0));

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "mixed.cuh"
+#include "sphere_share.cuh"
 
 namespace sqbem {
 
@@ -53,7 +54,9 @@ struct MixedSwimmer {
     int nsp = 0;                  // multiple of 128 >= ns
     DevBuf<float> B, AuBt;        // nt x ns
     DevBuf<float> D;              // ns x nt
-    DevBuf<float> E, AuBs;        // ns x ns
+    DevBuf<float> E, AuBs;        // ns x ns (E unused while `sphere` provides it)
+    std::shared_ptr<const SphereBlocks> sphere;  // the call's shared sphere-sphere blocks, if they fit
+    const float* e() const { return sphere ? sphere->E.get() : E.get(); }
     DevBuf<float> Ct, Cs;         // nt x 6, ns x 6
     DevBuf<float> Y;              // T^{-1} [B | Ct], nt x nc, leading dimension ldY
     long long ldY = 0;            // nt (explicit T^{-1}) or the padded ntp (the LU solve's buffer)
@@ -76,7 +79,10 @@ struct MixedCtx;
 // swimmers also equal sphere size).  The assembly runs per member, the dense
 // steps as grouped launches.
 void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx, bool explicit_inverse = true);
-void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx);
+// share (may be null): sphere-sphere blocks assembled once for the call; a
+// member whose sphere matches them copies / reads them instead of assembling.
+void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx& cx,
+                          const std::shared_ptr<const SphereBlocks>& share = nullptr);
 // Refined solve of every member for nrhs right-hand sides; x = [f_t; f_s; w]
 // per member (device, FP64, (nt + nc) x nrhs), plus the iterations used and the
 // final relative residual (max over members and right-hand sides).

@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "concurrent.cuh"
 #include "solver.cuh"
+#include "sphere_share.cuh"
 #include "tube_cache.cuh"
 
 using namespace sqbem;
@@ -66,6 +67,11 @@ public:
         R_ = a_ / P.a_over_R;
         tube_ = cached_tube(R_, P.L_over_R * R_, a_, P.n_theta, 4, 1.0, precision);
         sph0_ = bem::icosphere(a_, P.sphere_level);
+        if (precision == SQBEM_MIXED) {  // every evaluation of this call shares the sphere-sphere blocks
+            const auto V = mesh_vertices(sph0_);
+            const double c0[3] = {0, 0, 0};
+            share_ = build_sphere_blocks(make_panels(V.data(), sph0_.P()), c0, 1.0, st_);
+        }
     }
     // work on st_ that reads the shared tube ends before the reference is dropped
     ~Evaluator() { cudaStreamSynchronize(st_); }
@@ -120,7 +126,7 @@ public:
             DevBuf<int> flags(2, st);
             flags.zero();
             MixedCtx cx{st, flags.get(), flags.get() + 1};
-            mixed_build_swimmers(sp, cx);
+            mixed_build_swimmers(sp, cx, share_);
             // the slip modes on the device (slip_modes_group), solved in place
             std::vector<DevBuf<double>> din(G);
             gr.dx.clear();
@@ -220,6 +226,7 @@ private:
     double a_ = 1, R_ = 1;
     std::shared_ptr<const sqbem_tube> tube_;
     Stream st_;  // this evaluation's own stream (the cached tube's is not used)
+    std::shared_ptr<const SphereBlocks> share_;  // mixed: the sphere-sphere blocks of this call
     bem::Mesh sph0_;
     std::atomic<long long> evals_{0};
 };

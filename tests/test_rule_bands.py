@@ -69,3 +69,19 @@ def test_fp32_rule_bands_match_the_exact_rule(oracle, k):
         pairs += rb.size
         fallback += int((~decided).sum())
     assert fallback <= 1e-5 * pairs + 2, (fallback, pairs)
+
+
+def test_sphere_sphere_rules_are_translation_invariant(oracle):
+    """The mixed path shares one sphere-sphere block (built around the sphere's
+    centre) among all same-level instances of a call.  That holds only if the
+    reference's FP64 rule decisions for the translated sphere of every sweep
+    instance equal those of the centred sphere: checked here for every
+    instance of the sweep workload."""
+    a = 1.0
+    base = {lev: oracle.icosphere(a, lev, (0.0, 0.0, 0.0)) for lev in (2, 3)}
+    rules = {lev: exact_rule(S.centroid, S.centroid, S.h) for lev, S in base.items()}
+    for ins in workloads.sweep():
+        R = a / ins["a_over_R"]
+        b = ins["beta"] * (R - a)
+        S = oracle.icosphere(a, ins["sphere_level"], (b, 0.0, 0.0))
+        assert np.array_equal(exact_rule(S.centroid, S.centroid, S.h), rules[ins["sphere_level"]])
