@@ -130,14 +130,17 @@ __device__ __forceinline__ void put_split(bf16* h, bf16* l, long long i, float x
 // shared memory (with both inverses: 3 x 128 x 129 floats).
 //
 // LU, blocked right-looking with 16-column panels:
-//   panel   warps 0-3, each thread holding one row of the panel in registers
-//           for all 16 columns; the pivot row is broadcast through a
-//           double-buffered shared copy, one named barrier of those 128 threads
-//           per column (one warp alone is latency-bound; a CTA-wide barrier
-//           per column costs more than the arithmetic);
-//   U12     one thread per column solves with the unit-lower 16 x 16 block;
-//   A22     rank-16 update, 4 rows x 1 column per thread (columns across the
-//           warp: conflict-free; the row values are broadcasts).
+//   diag    warp 0 factors the 16 x 16 diagonal block, a row per lane, the
+//           pivot row broadcast by shuffles (no barrier per column);
+//   L21     the rows below, one per thread and independent of each other:
+//           l_ij = (a_ij - sum_{k<j} l_ik U_kj) / U_jj in registers; the
+//           certificate compares |a_ij - sum| with |U_jj| exactly (what partial
+//           pivoting compares), the multiplier uses the pivot's reciprocal;
+//   U12     at the same time, by other threads: one column per thread solves
+//           with the unit-lower 16 x 16 block, the column in registers;
+//   A22     rank-16 update in 4 x 4 register tiles: a warp takes 4 rows, a lane
+//           4 columns 32 apart (conflict-free loads of the U12 row, broadcasts
+//           of the L21 column), half a shared load per multiply-add.
 // Inverses: blocked by 16 with 4 x 4 register tiles (see below).
 struct DiagArgs {
     int* flag;
@@ -155,7 +158,6 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     float* rd = sh + 3 * N * DP;  // 1 / U(r, r)
     float(*tl)[DP] = reinterpret_cast<float(*)[DP]>(sh + 3 * N * DP + N);            // 16 x N scratch (L^{-1})
     float(*tu)[DP] = reinterpret_cast<float(*)[DP]>(sh + 3 * N * DP + N + DG_PW * DP);  // 16 x N scratch (U^{-1})
-    __shared__ float prow_buf[2][DG_PW];  // the panel's pivot row, double-buffered
     const DiagJob& J = args.j[blockIdx.x];
     const int tid = threadIdx.x;
     {
@@ -165,67 +167,115 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_kernel(const __grid_constan
     }
     __syncthreads();
     int bad = 0;
+    __shared__ float rinv[DG_PW];  // 1 / U(j, j) of the current panel
     for (int c0 = 0; c0 < N; c0 += DG_PW) {
-        if (tid < 128) {
-            // the panel, by warps 0-3: thread t keeps row c0 + t in registers for
-            // the whole panel (compile-time column indices); the owner of the
-            // pivot row publishes it to a double-buffered shared copy, and the
-            // four warps meet at a named barrier per column
-            const int i = c0 + tid;
+        if (tid < 32) {
+            // the 16 x 16 diagonal block by warp 0: lane t keeps row c0 + t in
+            // registers; the pivot row travels by shuffles (no barrier)
+            const int t = tid;
             float row[DG_PW];
 #pragma unroll
-            for (int cc = 0; cc < DG_PW; ++cc) row[cc] = i < N ? a[i][c0 + cc] : 0.f;
+            for (int cc = 0; cc < DG_PW; ++cc) row[cc] = t < DG_PW ? a[c0 + t][c0 + cc] : 0.f;
+#pragma unroll
             for (int jj = 0; jj < DG_PW; ++jj) {
-                float* pr = prow_buf[jj & 1];
-                if (tid == jj)
+                const float piv = __shfl_sync(0xffffffffu, row[jj], jj);
+                if (t == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
+                const float rp = 1.f / piv;
+                float pr[DG_PW];
 #pragma unroll
-                    for (int cc = 0; cc < DG_PW; ++cc) pr[cc] = row[cc];
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-                const float piv = pr[jj];
-                if (tid == 0 && !(piv != 0.f && isfinite(piv))) bad |= 2;
-                if (tid > jj && i < N) {
-                    float rj = row[0];
+                for (int cc = jj + 1; cc < DG_PW; ++cc) pr[cc] = __shfl_sync(0xffffffffu, row[cc], jj);
+                if (t > jj && t < DG_PW) {
+                    const float rj = row[jj];
+                    const float l = rj * rp;
+                    if (!(fabsf(rj) <= fabsf(piv))) bad |= isfinite(l) ? 1 : 2;
 #pragma unroll
-                    for (int cc = 1; cc < DG_PW; ++cc)
-                        if (cc == jj) rj = row[cc];
-                    const float l = rj / piv;
-                    if (!(fabsf(l) <= 1.f)) bad |= isfinite(l) ? 1 : 2;
+                    for (int cc = jj + 1; cc < DG_PW; ++cc) row[cc] = fmaf(-l, pr[cc], row[cc]);
+                    row[jj] = l;
+                }
+            }
+            if (t < DG_PW) {
+                float d = row[0];
 #pragma unroll
-                    for (int cc = 0; cc < DG_PW; ++cc) {
-                        if (cc > jj) row[cc] = fmaf(-l, pr[cc], row[cc]);
-                        else if (cc == jj) row[cc] = l;
+                for (int cc = 0; cc < DG_PW; ++cc) {
+                    a[c0 + t][c0 + cc] = row[cc];
+                    if (cc == t) d = row[cc];
+                }
+                rinv[t] = 1.f / d;
+            }
+        }
+        __syncthreads();
+        if (tid < 128) {
+            // L21: rows below the block, one per thread, independent of each other:
+            // l_ij = (a_ij - sum_{k<j} l_ik U_kj) / U_jj, certified |numerator| <= |U_jj|
+            const int i = c0 + DG_PW + tid;
+            if (i < N) {
+                float x[DG_PW];
+#pragma unroll
+                for (int j = 0; j < DG_PW; ++j) x[j] = a[i][c0 + j];
+#pragma unroll
+                for (int j = 0; j < DG_PW; ++j) {
+#pragma unroll
+                    for (int k = 0; k < j; ++k) x[j] = fmaf(-x[k], a[c0 + k][c0 + j], x[j]);
+                    const float u = a[c0 + j][c0 + j];
+                    const float l = x[j] * rinv[j];
+                    if (!(fabsf(x[j]) <= fabsf(u))) bad |= isfinite(l) ? 1 : 2;
+                    x[j] = l;
+                }
+#pragma unroll
+                for (int j = 0; j < DG_PW; ++j) a[i][c0 + j] = x[j];
+            }
+        } else if (tid < 256) {
+            // U12 = L11^{-1} A12 at the same time, one column per thread, in registers
+            const int c = c0 + DG_PW + (tid - 128);
+            if (c < N) {
+                float x[DG_PW];
+#pragma unroll
+                for (int r = 0; r < DG_PW; ++r) x[r] = a[c0 + r][c];
+#pragma unroll
+                for (int r = 1; r < DG_PW; ++r)
+#pragma unroll
+                    for (int k = 0; k < r; ++k) x[r] = fmaf(-a[c0 + r][c0 + k], x[k], x[r]);
+#pragma unroll
+                for (int r = 1; r < DG_PW; ++r) a[c0 + r][c] = x[r];
+            }
+        }
+        __syncthreads();
+        {  // A22 -= L21 U12 in 4 x 4 tiles: rows i0 .. i0 + 3 per warp, columns c1 + lane + 32 p
+            const int m = N - c0 - DG_PW, c1 = c0 + DG_PW;
+            const int warp = tid >> 5, lane = tid & 31;
+            for (int g = warp; g < m / 4; g += DIAG_THREADS / 32) {
+                const int i0 = c1 + 4 * g;
+                float acc[4][4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        const int c = c1 + lane + 32 * p;
+                        acc[q][p] = c < N ? a[i0 + q][c] : 0.f;
                     }
+#pragma unroll
+                for (int k = 0; k < DG_PW; ++k) {
+                    float lv[4], uv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) lv[q] = a[i0 + q][c0 + k];
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        const int c = c1 + lane + 32 * p;
+                        uv[p] = c < N ? a[c0 + k][c] : 0.f;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(-lv[q], uv[p], acc[q][p]);
                 }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        const int c = c1 + lane + 32 * p;
+                        if (c < N) a[i0 + q][c] = acc[q][p];
+                    }
             }
-            if (i < N)
-#pragma unroll
-                for (int cc = 0; cc < DG_PW; ++cc) a[i][c0 + cc] = row[cc];
-        }
-        __syncthreads();
-        {  // U12 = L11^{-1} A12
-            const int c = c0 + DG_PW + tid;
-            if (c < N)
-                for (int r = 1; r < DG_PW; ++r) {
-                    float v = a[c0 + r][c];
-                    for (int k = 0; k < r; ++k) v = fmaf(-a[c0 + r][c0 + k], a[c0 + k][c], v);
-                    a[c0 + r][c] = v;
-                }
-        }
-        __syncthreads();
-        const int m = N - c0 - DG_PW;  // A22 -= L21 U12
-        for (int e = tid; e < (m / 4) * m; e += DIAG_THREADS) {
-            const int c = c0 + DG_PW + e % m, i0 = c0 + DG_PW + 4 * (e / m);
-            float acc[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] = a[i0 + q][c];
-#pragma unroll
-            for (int k = 0; k < DG_PW; ++k) {
-                const float u = a[c0 + k][c];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) acc[q] = fmaf(-a[i0 + q][c0 + k], u, acc[q]);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) a[i0 + q][c] = acc[q];
         }
         __syncthreads();
     }
