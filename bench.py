@@ -442,7 +442,6 @@ def main():
     sqbem.set_limits(-1, -1)
     for _ in range(args.warmup):  # >= 3 for a valid bench line
         sqbem.kinematics_batch(insts, prec)
-    sqbem.kernel_stats_enable(True)
     launches0 = sqbem.launch_count()
     h2d0, d2h0 = sqbem.transfer_bytes()
     clocks = Clocks()
@@ -462,10 +461,6 @@ def main():
     gpu_s = allmax(dist, gpu_s)
     wall = allmax(dist, wall)
     solves = allsum(dist, float(len(insts) * args.steps))
-    # kernel classes of the timed region (per-launch CUDA events; with six
-    # concurrent streams a launch's duration includes co-scheduled kernels)
-    stats = {c: sqbem.kernel_stats(c) for c in sqbem.kernel_stats_classes()}
-    sqbem.kernel_stats_enable(False)
     step_s = gpu_s / args.steps
     # the kernels' own rates: the same workload once more, untimed, on a single
     # stream, every launch bracketed by CUDA events on its stream
@@ -580,8 +575,6 @@ def main():
         "assembly": assembly,
         "fp64_gpu": fp64,
         "cpu_baseline": cpu,
-        "kernel_stats": {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]}
-                         for c, v in stats.items()},
         "kernel_stats_single_stream": None if st1 is None else
         {c: {"launches": v[0], "seconds": v[1], "flops": v[2], "bytes": v[3]} for c, v in st1.items()},
     }

@@ -34,7 +34,6 @@ constexpr int MV_ROWS = 128;
 #endif
 constexpr int MV_CHUNK = SQBEM_MV_CHUNK;
 constexpr int MV_BATCH = SQBEM_MV_BATCH;  // matrix loads issued together before their products
-static_assert(MV_CHUNK % MV_BATCH == 0, "matvec chunk must be a multiple of the load batch");
 constexpr int MV_RMAX = 8;
 
 constexpr int MAXJOBS = 48;
@@ -71,10 +70,17 @@ __device__ __forceinline__ void dot2_step(float& s, float& c, float a, float xh,
     c = __fmaf_rn(a, xl, c);
 }
 
-template <int R>
+// PLAIN: one FP32 multiply-add per element and column (x rounded to FP32),
+// accumulated in FP32 within the chunk; for products whose error only enters a
+// correction: preconditioner applications and residual updates r -= A d with a
+// small d.  Without the compensation the kernel is HBM-bound, so it keeps
+// twice as many loads in flight.
+template <int R, bool PLAIN>
 __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ MvArgs args,
                                                         double* __restrict__ part) {
-    __shared__ float xs[R][2][MV_CHUNK];
+    constexpr int NB = PLAIN ? 2 * MV_BATCH : MV_BATCH;
+    static_assert(MV_CHUNK % NB == 0, "matvec chunk must be a multiple of the load batch");
+    __shared__ float xs[R][PLAIN ? 1 : 2][MV_CHUNK];
     const int jb = blockIdx.z, c = blockIdx.y;
     const int nchunk = args.j[jb].nchunk;
     if (c >= nchunk) return;
@@ -90,7 +96,7 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
         const double v = (k < r && j < nj) ? X[j0 + j + (long long)k * ldx] : 0.0;
         const float h = (float)v;
         xs[k][0][j] = h;
-        xs[k][1][j] = (float)(v - (double)h);
+        if (!PLAIN) xs[k][PLAIN ? 0 : 1][j] = (float)(v - (double)h);
     }
     __syncthreads();
     const int row = blockIdx.x * MV_ROWS + threadIdx.x;
@@ -99,16 +105,19 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
 #pragma unroll
     for (int k = 0; k < R; ++k) s[k] = cc[k] = 0.f;
     const float* a = A + row + (long long)j0 * lda;
-    // MV_BATCH independent loads in flight per thread; entries past the chunk
-    // read as 0 (and the staged vector is 0 there), adding nothing.
-    for (int j = 0; j < nj; j += MV_BATCH) {
-        float av[MV_BATCH];
+    // NB independent loads in flight per thread; entries past the chunk read as
+    // 0 (and the staged vector is 0 there), adding nothing.
+    for (int j = 0; j < nj; j += NB) {
+        float av[NB];
 #pragma unroll
-        for (int u = 0; u < MV_BATCH; ++u) av[u] = j + u < nj ? __ldg(a + (long long)(j + u) * lda) : 0.f;
+        for (int u = 0; u < NB; ++u) av[u] = j + u < nj ? __ldg(a + (long long)(j + u) * lda) : 0.f;
 #pragma unroll
-        for (int u = 0; u < MV_BATCH; ++u)
+        for (int u = 0; u < NB; ++u)
 #pragma unroll
-            for (int k = 0; k < R; ++k) dot2_step(s[k], cc[k], av[u], xs[k][0][j + u], xs[k][1][j + u]);
+            for (int k = 0; k < R; ++k) {
+                if (PLAIN) s[k] = fmaf(av[u], xs[k][0][j + u], s[k]);
+                else dot2_step(s[k], cc[k], av[u], xs[k][0][j + u], xs[k][PLAIN ? 0 : 1][j + u]);
+            }
     }
     double* o = part + poff + ((long long)c * m + row) * rstride;
 #pragma unroll
@@ -223,16 +232,17 @@ __global__ void sumsq_kernel(const __grid_constant__ NormArgs args) {
 
 static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st);
 
-// FP32 and FP64 matrices go to separate launches: one FP64 job would otherwise
-// move the whole launch onto the FP64 kernel.
+// Compensated FP32, plain FP32 and FP64 jobs go to separate launches: one job
+// of another kind would move the whole launch onto its kernel.
 void matvec_group(const std::vector<MvJob>& jobs_in, cudaStream_t st) {
-    std::vector<MvJob> j32, j64;
+    std::vector<MvJob> j32, j32p, j64;
     for (const MvJob& j : jobs_in)
         if (j.m > 0 && j.r > 0) {
             if (j.r > MV_RMAX) fail(SQBEM_ERR_ARG, "matvec: at most %d right-hand sides", MV_RMAX);
-            (j.A32 ? j32 : j64).push_back(j);
+            (j.A32 ? (j.plain ? j32p : j32) : j64).push_back(j);
         }
     matvec_launches(j32, st);
+    matvec_launches(j32p, st);
     matvec_launches(j64, st);
 }
 
@@ -261,15 +271,20 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
         for (int k = 0; k < a.n; ++k) all32 = all32 && a.j[k].j.A32 != nullptr;
         if (kstats_on()) {
             char note[96];
-            std::snprintf(note, sizeof note, "jobs=%d m=%d chunks=%d r=%d fp32=%d", a.n, maxm, maxc, maxr, (int)all32);
+            std::snprintf(note, sizeof note, "jobs=%d m=%d chunks=%d r=%d fp32=%d plain=%d", a.n, maxm, maxc, maxr,
+                          (int)all32, (int)(all32 && a.j[0].j.plain));
             kstat_note(note);
         }
-        if (all32) {
+        const bool plain = all32 && a.j[0].j.plain;
+        if (plain) {
+            if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<2, true>), grid, MV_ROWS, 0, st, a, part.get());
+            else TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<MV_RMAX, true>), grid, MV_ROWS, 0, st, a, part.get());
+        } else if (all32) {
             // the compensated sums are FP32-issue-bound, so the column count is a
             // template parameter (2: refinement; 6: the rigid-body columns A_u K)
-            if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<2>, grid, MV_ROWS, 0, st, a, part.get());
-            else if (maxr <= 6) TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<6>, grid, MV_ROWS, 0, st, a, part.get());
-            else TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial32<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
+            if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<2, false>), grid, MV_ROWS, 0, st, a, part.get());
+            else if (maxr <= 6) TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<6, false>), grid, MV_ROWS, 0, st, a, part.get());
+            else TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<MV_RMAX, false>), grid, MV_ROWS, 0, st, a, part.get());
         } else if (maxr <= 2) {
             TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<2>, grid, MV_ROWS, 0, st, a, part.get());
         } else {

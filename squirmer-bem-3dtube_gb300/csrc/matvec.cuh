@@ -22,6 +22,9 @@ struct MvJob {
     double* y = nullptr;
     long long ldy = 0;
     double alpha = 1, beta = 0;
+    // FP32 matrices only: plain FP32 multiply-adds instead of the compensated
+    // sum (for products whose error only enters a correction)
+    bool plain = false;
 };
 
 void matvec_group(const std::vector<MvJob>& jobs, cudaStream_t st);

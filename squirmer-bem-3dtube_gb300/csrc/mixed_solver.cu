@@ -149,6 +149,14 @@ MvJob mv32(const float* A, long long lda, int m, int n, const double* x, long lo
     j.alpha = alpha; j.beta = beta;
     return j;
 }
+// the same in plain FP32 (a preconditioner product or a residual update with a
+// small correction: its rounding enters only the next correction)
+MvJob mv32p(const float* A, long long lda, int m, int n, const double* x, long long ldx, int r, double* y,
+            long long ldy, double alpha, double beta) {
+    MvJob j = mv32(A, lda, m, n, x, ldx, r, y, ldy, alpha, beta);
+    j.plain = true;
+    return j;
+}
 MvJob mv64(const double* A, long long lda, int m, int n, const double* x, long long ldx, int r, double* y,
            long long ldy, double alpha, double beta) {
     MvJob j = mv32(nullptr, lda, m, n, x, ldx, r, y, ldy, alpha, beta);
@@ -546,6 +554,39 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             mj.clear();
         }
     };
+    // r -= A d for the correction d = [d_t; d_s; d_w] just added to x (in
+    // W.dt and W.dsw), in plain FP32: after the first step |d| is about 3e-5
+    // |x|, so the FP32 rounding of A d lies ~1e-11 below |b|, far under the
+    // stopping tolerance; the first step's residual (|d| = |x|) is formed from
+    // b with the compensated sums.
+    auto correct_residual = [&]() {
+        for (int round = 0; round < (prescribed ? 2 : 3); ++round) {
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const double* dt = W[k].dt.get();
+                const double* ds = W[k].dsw.get();
+                const double* dw = W[k].dsw.get() + M.ns;
+                double* rt = W[k].rt.get();
+                double* rs = W[k].rs.get();
+                if (round == 0) {
+                    if (bounded) {
+                        mj.push_back(mv32p(sw[k]->tube->mt.T.get(), M.nt, M.nt, M.nt, dt, M.nt, r, rt, M.nt, -1.0, 1.0));
+                        mj.push_back(mv32p(M.D.get(), M.ns, M.ns, M.nt, dt, M.nt, r, rs, M.ns, -1.0, 1.0));
+                    }
+                    if (!prescribed)
+                        mj.push_back(mv64(M.F.get(), 6, 6, M.ns, ds, M.nc, r, W[k].rc.get(), 6, -1.0, 1.0));
+                } else if (round == 1) {
+                    if (bounded) mj.push_back(mv32p(M.B.get(), M.nt, M.nt, M.ns, ds, M.nc, r, rt, M.nt, -1.0, 1.0));
+                    mj.push_back(mv32p(M.e(), M.ns, M.ns, M.ns, ds, M.nc, r, rs, M.ns, -1.0, 1.0));
+                } else {  // d_w is zero in the prescribed solve
+                    if (bounded) mj.push_back(mv32p(M.Ct.get(), M.nt, M.nt, 6, dw, M.nc, r, rt, M.nt, -1.0, 1.0));
+                    mj.push_back(mv32p(M.Cs.get(), M.ns, M.ns, 6, dw, M.nc, r, rs, M.ns, -1.0, 1.0));
+                }
+            }
+            matvec_group(mj, cx.st);
+            mj.clear();
+        }
+    };
     // |r|^2 per right-hand side (tube, sphere and constraint rows together)
     auto norms = [&]() {
         std::vector<NormJob> nj;
@@ -579,7 +620,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
             if (bounded && !factor_mode) {
                 const MixedTube& Tt = sw[k]->tube->mt;
-                mj.push_back(mv32(Tt.Ti.get(), Tt.ntp, M.nt, M.nt, W[k].rt.get(), M.nt, r, W[k].yt.get(), M.nt, 1.0, 0.0));
+                mj.push_back(mv32p(Tt.Ti.get(), Tt.ntp, M.nt, M.nt, W[k].rt.get(), M.nt, r, W[k].yt.get(), M.nt, 1.0, 0.0));
             }
         }
         copy_group(cj, cx.st);
@@ -602,7 +643,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         if (bounded) {
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                mj.push_back(mv32(M.D.get(), M.ns, M.ns, M.nt, W[k].yt.get(), M.nt, r, W[k].rsp.get(), M.ns, -1.0, 1.0));
+                mj.push_back(mv32p(M.D.get(), M.ns, M.ns, M.nt, W[k].yt.get(), M.nt, r, W[k].rsp.get(), M.ns, -1.0, 1.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();
@@ -660,7 +701,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
             cj.clear();
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
-                mj.push_back(mv32(M.Y.get(), M.ldY, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
+                mj.push_back(mv32p(M.Y.get(), M.ldY, M.nt, M.nc, W[k].dsw.get(), M.nc, r, W[k].dt.get(), M.nt, -1.0, 1.0));
             }
             matvec_group(mj, cx.st);
             mj.clear();
@@ -674,7 +715,8 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         copy_group(cj, cx.st);
         cj.clear();
         // (h) new residual
-        compute_residual(false);
+        if (it == 1) compute_residual(false);
+        else correct_residual();
         const std::vector<double> rn = norms();
         worst = 0;
         for (size_t k = 0; k < G * r; ++k) {

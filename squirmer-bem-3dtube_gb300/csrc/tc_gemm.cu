@@ -653,8 +653,11 @@ void tc_gemm(const std::vector<TcProblem>& probs_in, const std::vector<TcOperand
         a.probs[a.nprob++] = P;
         // tensor-pipe work: two or three BF16 products per element product
         flops += P.products * 2.0 * P.M * P.N * P.K;
-        bytes += ((P.products == 2 ? 2.0 : 4.0) * P.M * P.K + 4.0 * P.K * P.N) +
-                 4.0 * (P.beta != 0.f ? 2.0 : 1.0) * P.M * P.N;
+        // algorithmic bytes: each operand plane once, C read (beta != 0) and
+        // written, and every split-BF16 output pair (2 + 2 bytes per element)
+        bytes += (P.products == 2 ? 2.0 : 4.0) * P.M * P.K + 4.0 * P.K * P.N +
+                 ((P.C && P.beta != 0.f ? 4.0 : 0.0) + (P.C ? 4.0 : 0.0) + (P.O_hi ? 4.0 : 0.0) +
+                  (P.P_hi ? 4.0 : 0.0)) * P.M * P.N;
     }
     flush(flops, bytes);
 }
