@@ -193,6 +193,18 @@ int sqbem_tube_panels(const sqbem_tube* t, int* Nt);
 /* tube panels (9 doubles each) and tags (Nt each), host arrays */
 int sqbem_tube_mesh_get(const sqbem_tube* t, double* V, int* tags);
 void sqbem_tube_destroy(sqbem_tube* t);
+/* The tube mesh of these parameters is n_theta-fold rotationally symmetric
+ * (tube_mesh, src/utils/mesh.hpp:149-196, puts every node at an angle
+ * 2 pi i / n_theta), so the mixed path assembles the tube block from the rows
+ * of one sector and rotates 3 x 3 blocks for the others.  No counterpart in
+ * the reference.  sqbem_tube_symmetry (host only): *nb = panels per sector, 0
+ * if the mesh has no such symmetry; sector[p] and rep[p] (Nt each, may be
+ * NULL): panel p is representative rep[p] of sector 0 rotated by sector[p]
+ * sectors.  sqbem_tube_block_f32: the deflated FP32 tube block of the mixed
+ * path (3 Nt x 3 Nt, column-major) assembled directly (symmetric = 0) or from
+ * the rows of one sector (symmetric = 1); for tests. */
+int sqbem_tube_symmetry(double R, double L, double a, int n_theta, int n_r, int* nb, int* sector, int* rep);
+int sqbem_tube_block_f32(double R, double L, double a, int n_theta, int n_r, double mu, int symmetric, float* out);
 
 /* ---------------------------------------------------------------- swimmer
  * SwimmerSolver, src/swimmer.hpp:83-289.  create = constructor + build()

@@ -304,11 +304,12 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
     __syncthreads();
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     if (i >= job.nT) return;
+    const int self_p = job.same_mesh ? i : (job.self_of ? job.self_of[i] : -1);
     const double x = job.tgt[3 * i], y = job.tgt[3 * i + 1], z = job.tgt[3 * i + 2];
     for (int s = 0; s < ns; ++s) {
         const PanelRec& P = sp[s];
         const int p = p0 + s;
-        const int rule = (job.same_mesh && p == i) ? 4 : rule_of(P, x, y, z);
+        const int rule = p == self_p ? 4 : rule_of(P, x, y, z);
         if (rule != 0) {
             near_append(job, i, p, rule);
             if (job.rule_count) atomicAdd(job.rule_count + rule, 1);
@@ -417,9 +418,11 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
     const int i = blockIdx.x * FAR_TGT + threadIdx.x;
     const int nsi = i < job.nT ? ns : 0;  // targets past the end take part in the barriers only
     float xh = 0.f, yh = 0.f, zh = 0.f, xl = 0.f, yl = 0.f, zl = 0.f;
+    int self_p = -1;
     if (nsi > 0) {
         xh = tgtf[6 * i]; yh = tgtf[6 * i + 1]; zh = tgtf[6 * i + 2];
         xl = tgtf[6 * i + 3]; yl = tgtf[6 * i + 4]; zl = tgtf[6 * i + 5];
+        self_p = job.same_mesh ? i : (job.self_of ? job.self_of[i] : -1);
     }
     const float ss = (float)job.sscale, ds = (float)job.dscale;
     for (int s = 0; s < nsi; ++s) {
@@ -430,7 +433,7 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         const float bz = (F.chi[2] - zh) + (F.clo[2] - zl);
         const float d2 = bx * bx + by * by + bz * bz;
         int rule;
-        if (job.same_mesh && p == i) rule = 4;
+        if (p == self_p) rule = 4;
         else if (d2 > F.thhi[2]) rule = 0;
         else if (d2 < F.thlo[2] && d2 > F.thhi[1]) rule = 1;
         else if (d2 < F.thlo[1] && d2 > F.thhi[0]) rule = 2;

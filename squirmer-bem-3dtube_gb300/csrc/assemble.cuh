@@ -32,6 +32,9 @@ struct BlockJob {
     const PanelRec* src = nullptr;
     int nS = 0;
     int same_mesh = 0;  // target i is the centroid of source panel i -> self integral
+    // same_mesh == 0: target i is the centroid of source panel self_of[i] (self
+    // integral there; a negative entry: none); null: no target is a centroid
+    const int* self_of = nullptr;
     TO* S = nullptr;
     long long s_rs = 1, s_cs = 0;
     TO* D = nullptr;

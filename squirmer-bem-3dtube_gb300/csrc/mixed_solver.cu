@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -20,6 +21,7 @@
 #include "mixed.cuh"
 #include "mixed_solver.cuh"
 #include "solver.cuh"
+#include "tube_sym.cuh"
 
 namespace sqbem {
 
@@ -51,6 +53,12 @@ BlockJob<float> fjob(const DevPanels& tgt, const DevPanels& src, bool same, doub
     j.sscale = 1.0 / (EIGHT_PI * mu);
     j.dscale = -1.0 / EIGHT_PI;
     return j;
+}
+
+// SQBEM_TUBE_SYMMETRY=0 assembles every tube block directly (for comparisons)
+bool tube_symmetry_enabled() {
+    const char* e = std::getenv("SQBEM_TUBE_SYMMETRY");
+    return !(e && e[0] == '0');
 }
 
 int cap_pairs(int a, int b) { return (int)std::min<long long>((long long)a * b, 64LL << 20); }
@@ -207,8 +215,15 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
         M.ntp = lu[k].n;
         const int np = M.ntp;
         lu[k].A.zero();
-        auto job = fjob(t->panels, t->panels, true, t->mu, lu[k].A.get(), np, nullptr, 0);
-        assemble_block(job, cap_pairs(t->Nt, t->Nt), cx.st, true);
+        // the tube block from the rows of one sector where the mesh is
+        // rotationally symmetric (every tube this library meshes), else directly
+        const TubeSymmetry sym = tube_symmetry_enabled() ? tube_symmetry(t->host_panels, t->n_theta) : TubeSymmetry{};
+        if (sym.ok) {
+            assemble_tube_symmetric(t, sym, lu[k].A.get(), np, cx.st);
+        } else {
+            auto job = fjob(t->panels, t->panels, true, t->mu, lu[k].A.get(), np, nullptr, 0);
+            assemble_block(job, cap_pairs(t->Nt, t->Nt), cx.st, true);
+        }
         deflate<float>(lu[k].A.get(), 1, np, t->panels, t->mu, cx.st);
         pad_identity(lu[k].A.get(), np, M.nt, np, cx.st);
         M.T.alloc((size_t)M.nt * M.nt, cx.st);

@@ -59,6 +59,8 @@ SIGNATURES = {
     "sqbem_tube_panels": (_c_i, [_VP, _I]),
     "sqbem_tube_mesh_get": (_c_i, [_VP, _D, _I]),
     "sqbem_tube_destroy": (None, [_VP]),
+    "sqbem_tube_symmetry": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _I, _I, _I]),
+    "sqbem_tube_block_f32": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _c_d, _c_i, _VP]),
     "sqbem_swimmer_create": (_c_i, [_VP, _c_i, _D, _I, _D, _c_d, _c_i, ctypes.POINTER(_VP)]),
     "sqbem_swimmer_solve_free": (_c_i, [_VP, _c_i, _D, _D, _D, _D, _D]),
     "sqbem_swimmer_solve_prescribed": (_c_i, [_VP, _D, _D, _D, _D]),
@@ -412,6 +414,31 @@ def tube_mesh(R, z, n_theta, n_r):
 
 def swimmer_tube_mesh(R, L, a, n_theta, n_r=4):
     return _make_mesh(lib().sqbem_swimmer_tube_mesh, R, L, a, n_theta, n_r)
+
+
+def tube_symmetry(R, L, a, n_theta, n_r=4):
+    """sqbem_tube_symmetry: (nb, sector, rep) of the swimmer tube mesh -- panel
+    p is sector-0 representative rep[p] rotated by sector[p] sectors of 2 pi /
+    n_theta; nb = 0 (and None, None) if the mesh has no such symmetry."""
+    nb = ctypes.c_int(0)
+    _check(lib().sqbem_tube_symmetry(R, L, a, n_theta, n_r, ctypes.byref(nb), None, None))
+    if nb.value == 0:
+        return 0, None, None
+    n = nb.value * n_theta
+    sector = np.zeros(n, dtype=np.int32)
+    rep = np.zeros(n, dtype=np.int32)
+    _check(lib().sqbem_tube_symmetry(R, L, a, n_theta, n_r, ctypes.byref(nb), _ip(sector), _ip(rep)))
+    return nb.value, sector, rep
+
+
+def tube_block_f32(R, L, a, n_theta, n_r=4, mu=1.0, symmetric=True):
+    """sqbem_tube_block_f32: the mixed path's deflated FP32 tube block (3 Nt x
+    3 Nt), assembled from the rows of one sector or directly."""
+    Nt = swimmer_tube_mesh(R, L, a, n_theta, n_r).P
+    T = np.zeros((3 * Nt, 3 * Nt), dtype=np.float32, order="F")
+    _check(lib().sqbem_tube_block_f32(R, L, a, n_theta, n_r, mu, 1 if symmetric else 0,
+                                      T.ctypes.data_as(_VP)))
+    return T
 
 
 def icosphere(a, level, center=(0.0, 0.0, 0.0), tag=SPHERE):

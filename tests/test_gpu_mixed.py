@@ -99,3 +99,23 @@ def test_mixed_fp64_rsqrt_error_bound():
     ref = 1.0 / np.sqrt(x)
     err = np.abs(y - ref) / ref
     assert err.max() < 2e-13, err.max()
+
+
+@pytest.mark.parametrize("a_over_R,nth", [(0.3, 24), (0.6, 24), (0.1, 10)])
+def test_tube_block_from_one_sector_matches_direct_assembly(a_over_R, nth):
+    """the mixed path assembles the tube block from the rows of one sector and
+    rotates 3 x 3 blocks (the mesh is n_theta-fold symmetric); against the
+    direct FP32 assembly of every pair the entries differ by FP32 rounding only:
+    1e-6 of the matrix's largest entry, and per panel pair 2e-6 of the largest
+    entry of its 3 x 3 block (single entries of a block can cancel, so their own
+    relative error is no measure)"""
+    R = 1.0 / a_over_R
+    Ts = sqbem.tube_block_f32(R, 4 * R, 1.0, nth, symmetric=True)
+    Td = sqbem.tube_block_f32(R, 4 * R, 1.0, nth, symmetric=False)
+    scale = float(np.max(np.abs(Td)))
+    diff = np.abs(Ts.astype(np.float64) - Td)
+    assert np.max(diff) <= 1e-6 * scale, np.max(diff) / scale
+    n = Td.shape[0] // 3
+    bd = diff.reshape(n, 3, n, 3).max(axis=(1, 3))
+    bm = np.abs(Td.astype(np.float64)).reshape(n, 3, n, 3).max(axis=(1, 3))
+    assert np.max(bd / bm) <= 2e-6, np.max(bd / bm)
