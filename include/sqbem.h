@@ -205,6 +205,15 @@ void sqbem_tube_destroy(sqbem_tube* t);
  * the rows of one sector (symmetric = 1); for tests. */
 int sqbem_tube_symmetry(double R, double L, double a, int n_theta, int n_r, int* nb, int* sector, int* rep);
 int sqbem_tube_block_f32(double R, double L, double a, int n_theta, int n_r, double mu, int symmetric, float* out);
+/* Y = T^{-1} X (3 Nt x nc, column-major, host FP64) through the Fourier blocks
+ * of the tube: with every panel's vectors in its sector's frame T is
+ * block-circulant, and a DFT over the sectors splits it into n_theta / 2 + 1
+ * complex blocks of order 3 nb, which the mixed path inverts (FP32) and applies
+ * on the tensor cores instead of factoring T.  T is the block
+ * sqbem_tube_block_f32 returns with symmetric = 1; for tests.  No counterpart in
+ * the reference. */
+int sqbem_tube_fourier_solve(double R, double L, double a, int n_theta, int n_r, double mu, int nc, const double* X,
+                             double* Y);
 
 /* ---------------------------------------------------------------- swimmer
  * SwimmerSolver, src/swimmer.hpp:83-289.  create = constructor + build()

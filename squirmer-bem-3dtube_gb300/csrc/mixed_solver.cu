@@ -55,10 +55,16 @@ BlockJob<float> fjob(const DevPanels& tgt, const DevPanels& src, bool same, doub
     return j;
 }
 
-// SQBEM_TUBE_SYMMETRY=0 assembles every tube block directly (for comparisons)
+// SQBEM_TUBE_SYMMETRY=0 assembles every tube block directly and factors it
+// (for comparisons); SQBEM_TUBE_FOURIER=0 keeps the symmetric assembly but
+// factors the tube block instead of inverting its Fourier blocks.
 bool tube_symmetry_enabled() {
     const char* e = std::getenv("SQBEM_TUBE_SYMMETRY");
     return !(e && e[0] == '0');
+}
+bool tube_fourier_enabled() {
+    const char* e = std::getenv("SQBEM_TUBE_FOURIER");
+    return tube_symmetry_enabled() && !(e && e[0] == '0');
 }
 
 int cap_pairs(int a, int b) { return (int)std::min<long long>((long long)a * b, 64LL << 20); }
@@ -204,6 +210,36 @@ static void invert_group(const std::vector<MixedLU*>& L, const std::vector<float
 // ---------------------------------------------------------------- tubes
 void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx, bool explicit_inverse) {
     const size_t G = tubes.size();
+    // rotationally symmetric tubes (all of the group): the FP32 block for the
+    // residuals and the inverses of its Fourier blocks, no LU
+    std::vector<TubeSymmetry> syms(G);
+    bool four = tube_fourier_enabled() && G > 0;
+    for (size_t k = 0; k < G && four; ++k) {
+        syms[k] = tube_symmetry(tubes[k]->host_panels, tubes[k]->n_theta);
+        four = fourier_supported(syms[k]);
+    }
+    if (four) {
+        std::vector<DevBuf<float>> T0(G);
+        std::vector<FourierTube*> fts;
+        std::vector<const TubeSymmetry*> sp;
+        std::vector<const float*> t0p;
+        for (size_t k = 0; k < G; ++k) {
+            sqbem_tube* t = tubes[k];
+            MixedTube& M = t->mt;
+            M.nt = 3 * t->Nt;
+            M.ntp = pad128(M.nt);
+            M.T.alloc((size_t)M.nt * M.nt, cx.st);
+            assemble_tube_symmetric(t, syms[k], M.T.get(), M.nt, cx.st, &T0[k]);
+            M.lu.reset();
+            M.ft = std::make_unique<FourierTube>();
+            fts.push_back(M.ft.get());
+            sp.push_back(&syms[k]);
+            t0p.push_back(T0[k].get());
+        }
+        fourier_build(fts, sp, t0p, cx);
+        check_ctx(cx, "mixed tube (Fourier blocks)");
+        return;
+    }
     std::vector<MixedLU> lu(G);
     std::vector<MixedLU*> lus;
     std::vector<CopyJob> cj;
@@ -218,13 +254,13 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
         // the tube block from the rows of one sector where the mesh is
         // rotationally symmetric (every tube this library meshes), else directly
         const TubeSymmetry sym = tube_symmetry_enabled() ? tube_symmetry(t->host_panels, t->n_theta) : TubeSymmetry{};
-        if (sym.ok) {
+        if (sym.ok) {  // deflated from the sector-0 rows
             assemble_tube_symmetric(t, sym, lu[k].A.get(), np, cx.st);
         } else {
             auto job = fjob(t->panels, t->panels, true, t->mu, lu[k].A.get(), np, nullptr, 0);
             assemble_block(job, cap_pairs(t->Nt, t->Nt), cx.st, true);
+            deflate<float>(lu[k].A.get(), 1, np, t->panels, t->mu, cx.st);
         }
-        deflate<float>(lu[k].A.get(), 1, np, t->panels, t->mu, cx.st);
         pad_identity(lu[k].A.get(), np, M.nt, np, cx.st);
         M.T.alloc((size_t)M.nt * M.nt, cx.st);
         cj.push_back(cp32_32(lu[k].A.get(), np, M.T.get(), M.nt, M.nt, M.nt));
@@ -372,7 +408,34 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         // Y = T^{-1} [B | Ct]   (FP32 for the refinement, split for the Schur product)
         std::vector<TcProblem> P;
         std::vector<TcOperands> O;
-        if (!sw[0]->tube->mt.explicit_inverse()) {
+        for (size_t k = 1; k < G; ++k)
+            if (sw[k]->tube->mt.fourier() != sw[0]->tube->mt.fourier() ||
+                sw[k]->tube->mt.explicit_inverse() != sw[0]->tube->mt.explicit_inverse())
+                fail(SQBEM_ERR_ARG, "mixed swimmers of one group share a tube mode");
+        if (sw[0]->tube->mt.fourier()) {
+            // through the Fourier blocks; Y in its own buffer (ld nt), the split copy
+            // in (yh, yl) with ld ntp
+            std::vector<FourierJob> fj;
+            for (size_t k = 0; k < G; ++k) {
+                MixedSwimmer& M = sw[k]->mx;
+                const MixedTube& Tt = sw[k]->tube->mt;
+                const int ntp = Tt.ntp;
+                M.Y.alloc((size_t)M.nt * M.nc, cx.st);
+                M.ldY = M.nt;
+                FourierJob a;
+                a.ft = Tt.ft.get();
+                a.x32 = M.B.get(); a.ldx = M.nt; a.nc = M.ns;
+                a.y32 = M.Y.get(); a.ldy = M.nt;
+                a.yh = yh[k].get(); a.yl = yl[k].get(); a.lds = ntp;
+                fj.push_back(a);
+                FourierJob b = a;
+                b.x32 = M.Ct.get(); b.nc = 6;
+                b.y32 = M.Y.get() + (size_t)M.nt * M.ns;
+                b.yh = yh[k].get() + (size_t)ntp * M.ns; b.yl = yl[k].get() + (size_t)ntp * M.ns;
+                fj.push_back(b);
+            }
+            fourier_solve(fj, cx);
+        } else if (!sw[0]->tube->mt.explicit_inverse()) {
             // by the LU solves: X = [B | Ct] padded to ntp rows, solved in place; the
             // solves keep the column-major split copy (yh, yl) equal to the result
             std::vector<DevBuf<float>> yp(G);
@@ -381,7 +444,6 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             for (size_t k = 0; k < G; ++k) {
                 MixedSwimmer& M = sw[k]->mx;
                 const MixedTube& Tt = sw[k]->tube->mt;
-                if (Tt.explicit_inverse()) fail(SQBEM_ERR_ARG, "mixed swimmers of one group share a tube mode");
                 const int ntp = Tt.ntp;
                 yp[k].alloc((size_t)ntp * M.nc, cx.st);
                 if (ntp > M.nt)  // rows nt .. ntp of every column; the copies below fill the rest
@@ -499,7 +561,8 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
     struct Work {
         DevBuf<double> bt, bs, rt, rs, rc, rsp, yt, tmp6, dsw, dt, nrm;
     };
-    const bool factor_mode = bounded && !sw[0]->tube->mt.explicit_inverse();
+    const bool fourier_mode = bounded && sw[0]->tube->mt.fourier();
+    const bool factor_mode = bounded && !fourier_mode && !sw[0]->tube->mt.explicit_inverse();
     std::vector<Work> W(G);
     std::vector<MvJob> mj;
     std::vector<CopyJob> cj;
@@ -633,7 +696,7 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
         for (size_t k = 0; k < G; ++k) {
             MixedSwimmer& M = sw[k]->mx;
             cj.push_back(cp64(W[k].rs.get(), M.ns, W[k].rsp.get(), M.ns, M.ns, r));
-            if (bounded && !factor_mode) {
+            if (bounded && !factor_mode && !fourier_mode) {
                 const MixedTube& Tt = sw[k]->tube->mt;
                 mj.push_back(mv32p(Tt.Ti.get(), Tt.ntp, M.nt, M.nt, W[k].rt.get(), M.nt, r, W[k].yt.get(), M.nt, 1.0, 0.0));
             }
@@ -654,6 +717,17 @@ void mixed_solve(const std::vector<sqbem_swimmer*>& sw, bool prescribed, const s
                 nts.push_back(sw[k]->mx.nt);
             }
             trsv_group(tl, ins, outs, nts, r, cx.st);
+        }
+        if (fourier_mode) {  // y_t through the tube's Fourier blocks
+            std::vector<FourierJob> fj;
+            for (size_t k = 0; k < G; ++k) {
+                FourierJob a;
+                a.ft = sw[k]->tube->mt.ft.get();
+                a.x64 = W[k].rt.get(); a.ldx = sw[k]->mx.nt; a.nc = r;
+                a.y64 = W[k].yt.get(); a.ldy = sw[k]->mx.nt;
+                fj.push_back(a);
+            }
+            fourier_solve(fj, cx);
         }
         if (bounded) {
             for (size_t k = 0; k < G; ++k) {

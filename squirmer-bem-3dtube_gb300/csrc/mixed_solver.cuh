@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "mixed.cuh"
 #include "sphere_share.cuh"
+#include "tube_fourier.cuh"
 
 namespace sqbem {
 
@@ -46,7 +47,12 @@ struct MixedTube {
     // ... or, for a tube used by one swimmer (the batches), its factor only: Y and
     // the refinement's T^{-1} r come from LU solves, which saves forming T^{-1}
     std::unique_ptr<MixedLU> lu;  // split factor and diagonal-block inverses (A, Ch, Cl released)
-    bool explicit_inverse() const { return !lu; }
+    // ... or, for a rotationally symmetric tube (every tube this library meshes),
+    // the inverses of its Fourier blocks: T^{-1} X is a transform, one small GEMM
+    // per frequency and the inverse transform, for one swimmer or many
+    std::unique_ptr<FourierTube> ft;
+    bool fourier() const { return ft != nullptr; }
+    bool explicit_inverse() const { return !lu && !ft; }
 };
 
 struct MixedSwimmer {

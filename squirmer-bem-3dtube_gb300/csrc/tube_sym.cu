@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "mixed.cuh"
 #include "solver.cuh"
+#include "tube_fourier.cuh"
 #include "tube_sym.cuh"
 
 namespace sqbem {
@@ -106,10 +107,23 @@ __global__ void tube_fill_kernel(float* __restrict__ T, long long ld, const floa
     }
 }
 
+// Deflation of the sector-0 rows (swimmer.hpp:64-74, as deflate_kernel does for
+// the whole block): T0[3a + al, 3q + b] += sc n_rep(a)[al] n_q[b] area_q.
+__global__ void deflate_rows_kernel(float* __restrict__ T0, int ld0, const int* __restrict__ rep_panel, int nb,
+                                    const PanelRec* __restrict__ P, int Nt, double sc) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;  // row of T0
+    const int c = blockIdx.y;                             // column of T0
+    if (r >= 3 * nb) return;
+    const int i = rep_panel[r / 3], al = r % 3, q = c / 3, b = c % 3;
+    const double v = sc * P[i].n[al] * P[q].n[b] * P[q].area;
+    float* e = T0 + r + (long long)c * ld0;
+    *e = (float)((double)*e + v);
+}
+
 }  // namespace
 
 void assemble_tube_symmetric(const sqbem_tube* t, const TubeSymmetry& sym, float* T, long long ld,
-                             cudaStream_t st) {
+                             cudaStream_t st, DevBuf<float>* T0_out) {
     const int Nt = t->Nt, nb = sym.nb, nth = sym.nth;
     if (!sym.ok || nb * nth != Nt) fail(SQBEM_ERR_ARG, "tube assembly: the panels have no rotational symmetry");
     // rows of sector 0: targets are the representatives' centroids, sources all panels
@@ -135,6 +149,9 @@ void assemble_tube_symmetric(const sqbem_tube* t, const TubeSymmetry& sym, float
     j.sscale = 1.0 / (EIGHT_PI * t->mu);
     j.dscale = -1.0 / EIGHT_PI;
     assemble_block(j, (int)std::min<long long>((long long)nb * Nt, 64LL << 20), st, true);
+    const double sc = 1.0 / (EIGHT_PI * t->mu * std::sqrt(t->panels.area_total));
+    LAUNCH(deflate_rows_kernel, dim3(ceil_div(ld0, 128), 3 * Nt), 128, 0, st, T0.get(), ld0, self.get(), nb,
+           t->panels.rec.get(), Nt, sc);
     // the rotation of every sector and the panel maps
     std::vector<float2> hr(nth);
     const double al = 2.0 * 3.14159265358979323846 / nth;
@@ -148,6 +165,7 @@ void assemble_tube_symmetric(const sqbem_tube* t, const TubeSymmetry& sym, float
     const double bytes = 4.0 * 9.0 * Nt * (double)Nt;
     TIMED_LAUNCH("tube_fill", 0.0, bytes, tube_fill_kernel, dim3(ceil_div(Nt, 128), Nt), 128, 0, st, T, ld, T0.get(),
                  ld0, Nt, nth, sector.get(), rep.get(), panel.get(), rot.get());
+    if (T0_out) *T0_out = std::move(T0);
 }
 
 }  // namespace sqbem
@@ -171,7 +189,7 @@ extern "C" int sqbem_tube_block_f32(double R, double L, double a, int n_theta, i
         const int n = 3 * t.Nt;
         DevBuf<float> T((size_t)n * n, t.st);
         T.zero();
-        if (symmetric) {
+        if (symmetric) {  // deflated from the sector-0 rows
             const TubeSymmetry sym = tube_symmetry(t.host_panels, n_theta);
             assemble_tube_symmetric(&t, sym, T.get(), n, t.st);
         } else {
@@ -187,8 +205,8 @@ extern "C" int sqbem_tube_block_f32(double R, double L, double a, int n_theta, i
             j.sscale = 1.0 / (EIGHT_PI * mu);
             j.dscale = -1.0 / EIGHT_PI;
             assemble_block(j, (int)std::min<long long>((long long)t.Nt * t.Nt, 64LL << 20), t.st, true);
+            deflate<float>(T.get(), 1, n, t.panels, mu, t.st);
         }
-        deflate<float>(T.get(), 1, n, t.panels, mu, t.st);
         T.download(out, (size_t)n * n);
         CUDA_CHECK(cudaStreamSynchronize(t.st));
     });
@@ -208,5 +226,46 @@ extern "C" int sqbem_tube_symmetry(double R, double L, double a, int n_theta, in
         if (!S.ok) return;
         if (sector) std::copy(S.sector.begin(), S.sector.end(), sector);
         if (rep) std::copy(S.rep.begin(), S.rep.end(), rep);
+    });
+}
+
+// Y = T^{-1} X through the Fourier blocks of the tube of these parameters (X, Y:
+// 3 Nt x nc, column-major, host FP64), T the deflated FP32 block that
+// sqbem_tube_block_f32 returns with symmetric = 1; for tests of the Fourier
+// path.  No counterpart in the reference.
+extern "C" int sqbem_tube_fourier_solve(double R, double L, double a, int n_theta, int n_r, double mu, int nc,
+                                        const double* X, double* Y) {
+    return guarded([&] {
+        if (!X || !Y || nc < 1 || !(R > 0) || !(L > 0) || n_theta < 3 || n_r < 1 || !(mu > 0))
+            fail(SQBEM_ERR_ARG, "tube_fourier_solve: bad arguments");
+        require_device();
+        sqbem_tube t;
+        t.R = R; t.L = L; t.a = a; t.n_theta = n_theta; t.n_r = n_r; t.mu = mu;
+        t.precision = SQBEM_MIXED;
+        t.mesh = bem::swimmer_tube_mesh(R, L, a, n_theta, n_r);
+        t.set_panels();
+        const TubeSymmetry sym = tube_symmetry(t.host_panels, n_theta);
+        if (!fourier_supported(sym)) fail(SQBEM_ERR_ARG, "tube_fourier_solve: no Fourier path for this tube");
+        const int n = 3 * t.Nt;
+        DevBuf<float> T((size_t)n * n, t.st), T0;
+        assemble_tube_symmetric(&t, sym, T.get(), n, t.st, &T0);
+        DevBuf<int> flags(2, t.st);
+        flags.zero();
+        MixedCtx cx{t.st, flags.get(), flags.get() + 1};
+        FourierTube ft;
+        fourier_build({&ft}, {&sym}, {T0.get()}, cx);
+        DevBuf<double> dx((size_t)n * nc, t.st), dy((size_t)n * nc, t.st);
+        dx.upload(X, (size_t)n * nc);
+        FourierJob j;
+        j.ft = &ft;
+        j.x64 = dx.get(); j.ldx = n; j.nc = nc;
+        j.y64 = dy.get(); j.ldy = n;
+        fourier_solve({j}, cx);
+        dy.download(Y, (size_t)n * nc);
+        int h[2] = {};
+        flags.download(h, 2);
+        CUDA_CHECK(cudaStreamSynchronize(t.st));
+        if (h[0]) fail(SQBEM_ERR_TIMEOUT, "tube_fourier_solve: a bounded wait in the tensor-core GEMM expired");
+        if (h[1] & 2) fail(SQBEM_ERR_SINGULAR, "tube_fourier_solve: zero pivot in a Fourier block");
     });
 }

@@ -38,9 +38,11 @@ struct TubeSymmetry {
 TubeSymmetry tube_symmetry(const std::vector<PanelRec>& P, int nth);
 
 // T (FP32, column-major, leading dimension ld, 3 Nt x 3 Nt) <- the tube's
-// single-layer block SL / (8 pi mu) from the rows of sector 0, in the mixed
-// path's FP32 arithmetic (no deflation, which the caller adds).
+// deflated single-layer block SL / (8 pi mu) + (8 pi mu sqrt(A))^{-1} m_i m_p^T A_p
+// (src/swimmer.hpp:48-74) from the rows of sector 0, in the mixed path's FP32
+// arithmetic.  T0_out (optional) receives those rows: 3 nb x 3 Nt,
+// column-major, leading dimension 3 nb.
 void assemble_tube_symmetric(const sqbem_tube* t, const TubeSymmetry& sym, float* T, long long ld,
-                             cudaStream_t st);
+                             cudaStream_t st, DevBuf<float>* T0_out = nullptr);
 
 }  // namespace sqbem

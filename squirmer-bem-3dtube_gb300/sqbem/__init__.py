@@ -61,6 +61,7 @@ SIGNATURES = {
     "sqbem_tube_destroy": (None, [_VP]),
     "sqbem_tube_symmetry": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _I, _I, _I]),
     "sqbem_tube_block_f32": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _c_d, _c_i, _VP]),
+    "sqbem_tube_fourier_solve": (_c_i, [_c_d, _c_d, _c_d, _c_i, _c_i, _c_d, _c_i, _D, _D]),
     "sqbem_swimmer_create": (_c_i, [_VP, _c_i, _D, _I, _D, _c_d, _c_i, ctypes.POINTER(_VP)]),
     "sqbem_swimmer_solve_free": (_c_i, [_VP, _c_i, _D, _D, _D, _D, _D]),
     "sqbem_swimmer_solve_prescribed": (_c_i, [_VP, _D, _D, _D, _D]),
@@ -439,6 +440,15 @@ def tube_block_f32(R, L, a, n_theta, n_r=4, mu=1.0, symmetric=True):
     _check(lib().sqbem_tube_block_f32(R, L, a, n_theta, n_r, mu, 1 if symmetric else 0,
                                       T.ctypes.data_as(_VP)))
     return T
+
+
+def tube_fourier_solve(R, L, a, n_theta, X, n_r=4, mu=1.0):
+    """sqbem_tube_fourier_solve: T^{-1} X through the tube's Fourier blocks (X:
+    3 Nt x nc)."""
+    X = np.asfortranarray(X, dtype=np.float64)
+    Y = np.zeros_like(X, order="F")
+    _check(lib().sqbem_tube_fourier_solve(R, L, a, n_theta, n_r, mu, X.shape[1], _dp(X), _dp(Y)))
+    return Y
 
 
 def icosphere(a, level, center=(0.0, 0.0, 0.0), tag=SPHERE):
