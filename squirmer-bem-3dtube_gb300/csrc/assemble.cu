@@ -491,16 +491,30 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
 // Each pair is computed whole by one warp, so the result does not depend on the
 // order.
 template <class TO, bool MIXED>
-__global__ void __launch_bounds__(256, 3) near_kernel(BlockJob<TO> job) {
+__global__ void __launch_bounds__(32, 24) near_kernel(BlockJob<TO> job) {
     const int lane = threadIdx.x & 31;
     const int nh = job.near_count[0], nl = job.near_count[1];
     if (nh + nl > job.near_cap) return;  // overflow: reported by the host
-    const int count = nh + nl;
+    // heavy pairs (448-point rule, self integrals) by warp index: warp g takes
+    // g, g + W, ...; one-warp CTAs are dispatched round-robin over the SMs, so
+    // consecutive heavy pairs run on different SMs' FP64 pipes (a shared counter
+    // hands consecutive tickets to the warps of one SM).  Then the light pairs
+    // from the counter.
+    const int W = gridDim.x * (blockDim.x >> 5);
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int kh = gw;
     for (;;) {
-        int k = 0;
-        if (lane == 0) k = atomicAdd(job.near_count + 2, 1);
-        k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= count) break;
+        int k;
+        if (kh < nh) {
+            k = kh;
+            kh += W;
+        } else {
+            int t = 0;
+            if (lane == 0) t = atomicAdd(job.near_count + 2, 1);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t >= nl) break;
+            k = nh + t;
+        }
         const int2 e = job.near_list[k < nh ? k : job.near_cap - 1 - (k - nh)];
         const int i = e.x, p = e.y & 0x0fffffff;
         const PanelRec P = job.src[p];
@@ -567,7 +581,10 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
         CUDA_CHECK(cudaGetDevice(&dev));
         CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     });
-    const int warps = sms * 24;  // 3 CTAs of 8 warps per SM (80 registers per thread)
+    // 24 one-warp CTAs per SM (80 registers per thread): consecutive pairs of the
+    // list -- the heavy 448-point and self pairs come first -- go to warps of
+    // different SMs, so they do not queue on a few SMs' FP64 pipes
+    const int warps = sms * 24;
     // credited FP64-pipe work of the near kernel (kernel statistics only, which
     // count the pairs per rule on the device): the 448-point rule and the self
     // integral, plus in FP64 mode the 28- and 112-point rules (FP32 in mixed mode)
@@ -580,13 +597,13 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
         std::snprintf(note, sizeof note, "nT=%d nS=%d same=%d mixed=%d", job.nT, job.nS, job.same_mesh, (int)mixed);
         kstat_note(note);
         const int ks = kstat_begin(st);
-        if (mixed) LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
-        else LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
+        if (mixed) LAUNCH((near_kernel<TO, true>), warps, 32, 0, st, job);
+        else LAUNCH((near_kernel<TO, false>), warps, 32, 0, st, job);
         kstat_end_counted(ks, "assemble_near", st, counts, w, 5, 0.0);
     } else if (mixed) {
-        LAUNCH((near_kernel<TO, true>), warps * 32 / 256, 256, 0, st, job);
+        LAUNCH((near_kernel<TO, true>), warps, 32, 0, st, job);
     } else {
-        LAUNCH((near_kernel<TO, false>), warps * 32 / 256, 256, 0, st, job);
+        LAUNCH((near_kernel<TO, false>), warps, 32, 0, st, job);
     }
     if ((long long)job.nT * job.nS > near_cap) {
         // the list could overflow only for blocks larger than its capacity

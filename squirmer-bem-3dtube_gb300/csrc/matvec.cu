@@ -175,6 +175,89 @@ __global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __r
     }
 }
 
+// ---------------------------------------------------------------- rigid-body columns
+// y = A K chunk by chunk (RG_PANELS panels = 3 RG_PANELS columns per CTA column
+// block), partial sums per chunk, added in chunk order by rigid_finish.
+constexpr int RG_PANELS = 32;
+struct RigidDev {
+    RigidJob j;
+    long long part_off;
+    int nchunk;
+};
+struct RigidArgs {
+    int n;
+    RigidDev j[MAXJOBS];
+};
+
+// error-free s + a -> (s, c): the compensated sum of the translation columns
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float a) {
+    const float t = __fadd_rn(s, a);
+    const float z = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(a, z)));
+    s = t;
+}
+
+__global__ void __launch_bounds__(MV_ROWS) rigid_partial(const __grid_constant__ RigidArgs args,
+                                                         double* __restrict__ part) {
+    // per panel of the chunk: r (hi, lo) for the rotation entries
+    __shared__ float rh[RG_PANELS][3], rl[RG_PANELS][3];
+    const RigidDev& D = args.j[blockIdx.z];
+    const int c = blockIdx.y;
+    if (c >= D.nchunk) return;
+    const int p0 = c * RG_PANELS, np = min(D.j.np, p0 + RG_PANELS) - p0;
+    for (int e = threadIdx.x; e < 3 * RG_PANELS; e += blockDim.x) {
+        const int q = e / 3, k = e - 3 * q;
+        const double v = q < np ? D.j.rc[3 * (p0 + q) + k] : 0.0;
+        const float h = (float)v;
+        rh[q][k] = h;
+        rl[q][k] = (float)(v - (double)h);
+    }
+    __syncthreads();
+    const int row = blockIdx.x * MV_ROWS + threadIdx.x;
+    if (row >= D.j.m) return;
+    float s[6], cc[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s[k] = cc[k] = 0.f;
+    const float* a = D.j.A + row + (long long)(3 * p0) * D.j.lda;
+    const long long lda = D.j.lda;
+    for (int q0 = 0; q0 < np; q0 += 4) {
+        float av[12];
+#pragma unroll
+        for (int u = 0; u < 12; ++u) av[u] = q0 + u / 3 < np ? __ldg(a + (long long)(3 * q0 + u) * lda) : 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u;
+            if (q >= np) break;
+            const float x = av[3 * u], y = av[3 * u + 1], z = av[3 * u + 2];
+            two_sum_acc(s[0], cc[0], x);
+            two_sum_acc(s[1], cc[1], y);
+            two_sum_acc(s[2], cc[2], z);
+            // column 3 (e_x x r): -rz a_y + ry a_z; 4 (e_y x r): rz a_x - rx a_z;
+            // 5 (e_z x r): -ry a_x + rx a_y
+            dot2_step(s[3], cc[3], y, -rh[q][2], -rl[q][2]);
+            dot2_step(s[3], cc[3], z, rh[q][1], rl[q][1]);
+            dot2_step(s[4], cc[4], x, rh[q][2], rl[q][2]);
+            dot2_step(s[4], cc[4], z, -rh[q][0], -rl[q][0]);
+            dot2_step(s[5], cc[5], x, -rh[q][1], -rl[q][1]);
+            dot2_step(s[5], cc[5], y, rh[q][0], rl[q][0]);
+        }
+    }
+    double* o = part + D.part_off + ((long long)c * D.j.m + row) * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = (double)s[k] + (double)cc[k];
+}
+
+__global__ void rigid_finish(const __grid_constant__ RigidArgs args, const double* __restrict__ part) {
+    const RigidDev& D = args.j[blockIdx.y];
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= D.j.m) return;
+    for (int k = 0; k < 6; ++k) {
+        double t = 0.0;
+        for (int c = 0; c < D.nchunk; ++c) t += part[D.part_off + ((long long)c * D.j.m + row) * 6 + k];
+        D.j.y[row + (long long)k * D.j.ldy] = t;
+    }
+}
+
 // blockIdx.x: 256 rows, blockIdx.y: job, blockIdx.z: every gridDim.z-th column
 // (no per-element division; consecutive threads walk a column)
 __global__ void copy_kernel_g(const __grid_constant__ CopyArgs args) {
@@ -291,6 +374,33 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
             TIMED_LAUNCH("matvec", 0.0, bytes, mv_partial<MV_RMAX>, grid, MV_ROWS, 0, st, a, part.get());
         }
         LAUNCH(mv_finish, dim3(ceil_div(maxm, 128), (unsigned)a.n), 128, 0, st, a, part.get());
+    }
+}
+
+void rigid_product_group(const std::vector<RigidJob>& jobs_in, cudaStream_t st) {
+    std::vector<RigidJob> jobs;
+    for (const RigidJob& j : jobs_in)
+        if (j.m > 0 && j.np > 0) jobs.push_back(j);
+    for (size_t i0 = 0; i0 < jobs.size(); i0 += MAXJOBS) {
+        RigidArgs a;
+        a.n = (int)std::min<size_t>(MAXJOBS, jobs.size() - i0);
+        long long off = 0;
+        int maxm = 0, maxc = 0;
+        double bytes = 0;
+        for (int k = 0; k < a.n; ++k) {
+            const RigidJob& j = jobs[i0 + k];
+            a.j[k].j = j;
+            a.j[k].nchunk = ceil_div(j.np, RG_PANELS);
+            a.j[k].part_off = off;
+            off += (long long)a.j[k].nchunk * j.m * 6;
+            maxm = std::max(maxm, j.m);
+            maxc = std::max(maxc, a.j[k].nchunk);
+            bytes += 4.0 * j.m * 3.0 * j.np;
+        }
+        DevBuf<double> part((size_t)off, st);
+        TIMED_LAUNCH("matvec", 0.0, bytes, rigid_partial, dim3(ceil_div(maxm, MV_ROWS), maxc, (unsigned)a.n), MV_ROWS, 0,
+                     st, a, part.get());
+        LAUNCH(rigid_finish, dim3(ceil_div(maxm, 128), (unsigned)a.n), 128, 0, st, a, part.get());
     }
 }
 

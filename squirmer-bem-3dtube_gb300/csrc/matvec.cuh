@@ -29,6 +29,23 @@ struct MvJob {
 
 void matvec_group(const std::vector<MvJob>& jobs, cudaStream_t st);
 
+// y (m x 6, FP64, leading dimension ldy) = A K for the rigid-body map K of a
+// sphere (swimmer.hpp:224-231): A (m x 3 Ns, FP32, column-major, lda), K's row
+// 3p + b has 1 in column b and the entries of e_c x r_p in the rotation columns
+// c = 3, 4, 5 (r_p = centroid of panel p - sphere centre, 3 per panel in rc).
+// Compensated FP32 sums like the matvec: per element one error-free sum for
+// the translation column and two compensated products for the rotation columns
+// (K's zero entries are skipped).
+struct RigidJob {
+    const float* A = nullptr;
+    long long lda = 0;
+    int m = 0, np = 0;  // rows, panels (3 np columns)
+    const double* rc = nullptr;
+    double* y = nullptr;
+    long long ldy = 0;
+};
+void rigid_product_group(const std::vector<RigidJob>& jobs, cudaStream_t st);
+
 // Elementwise helpers on column-major FP64 / FP32 blocks of a group.
 struct CopyJob {
     const double* s64 = nullptr;  // one of s64 / s32 as source

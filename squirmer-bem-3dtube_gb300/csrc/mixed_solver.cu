@@ -302,8 +302,9 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
     const bool bounded = sw[0]->tube != nullptr;
     std::vector<CopyJob> cj;
     std::vector<MvJob> mj;
+    std::vector<RigidJob> rj;
     std::vector<DevBuf<double>> tmp;
-    tmp.reserve(2 * G);
+    tmp.reserve(3 * G);
     for (sqbem_swimmer* s : sw) {
         MixedSwimmer& M = s->mx;
         const int Ns = s->Ns, Nt = s->Nt;
@@ -347,14 +348,21 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         const auto Kh = rigid_map(s->host_panels, s->xc);
         M.K.alloc(Kh.size(), cx.st);
         M.K.upload(Kh.data(), Kh.size());
+        // (the panel offsets r_p = c_p - x_c give K's rotation entries)
+        std::vector<double> rch(3 * (size_t)Ns);
+        for (int p = 0; p < Ns; ++p)
+            for (int k = 0; k < 3; ++k) rch[3 * p + k] = s->host_panels[p].c[k] - s->xc[k];
+        tmp.emplace_back(rch.size(), cx.st);
+        tmp.back().upload(rch.data(), rch.size());
+        const double* rc = tmp.back().get();
         M.Cs.alloc((size_t)ns * 6, cx.st);
         tmp.emplace_back((size_t)ns * 6, cx.st);
-        mj.push_back(mv32(M.AuBs.get(), ns, ns, ns, M.K.get(), ns, 6, tmp.back().get(), ns, 1.0, 0.0));
+        rj.push_back({M.AuBs.get(), ns, ns, Ns, rc, tmp.back().get(), ns});
         cj.push_back(cp64_32(tmp.back().get(), ns, M.Cs.get(), ns, ns, 6));
         if (bounded) {
             M.Ct.alloc((size_t)nt * 6, cx.st);
             tmp.emplace_back((size_t)nt * 6, cx.st);
-            mj.push_back(mv32(M.AuBt.get(), nt, nt, ns, M.K.get(), ns, 6, tmp.back().get(), nt, 1.0, 0.0));
+            rj.push_back({M.AuBt.get(), nt, nt, Ns, rc, tmp.back().get(), nt});
             cj.push_back(cp64_32(tmp.back().get(), nt, M.Ct.get(), nt, nt, 6));
         }
         const auto F = constraint_rows(s->host_panels, s->xc, 1.0);
@@ -362,6 +370,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         M.F.upload(F.data(), F.size());
     }
     matvec_group(mj, cx.st);
+    rigid_product_group(rj, cx.st);
     copy_group(cj, cx.st);
     cj.clear();
     mj.clear();

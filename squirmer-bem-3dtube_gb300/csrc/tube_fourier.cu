@@ -115,25 +115,29 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gj_k
     bool bad = false;
     for (int k = 0; k < n; ++k) {
         const int buf = k & 1;
-        if (rank == k / w && warp == 0) {
+        if (rank == k / w) {
             const float2* ca = A + (size_t)(k - c0) * n;
-            float best = -1.f;
-            int bi = k;
-            for (int i = k + lane; i < n; i += 32) {
-                const float2 v = ca[i];
-                const float m = v.x * v.x + v.y * v.y;
-                if (m > best) { best = m; bi = i; }
+            // every thread copies a share of the column into every CTA; warp 0 also
+            // finds the pivot row
+            for (int e = threadIdx.x; e < CL * n; e += blockDim.x) {
+                const int q = e / n, i = e - q * n;
+                cl.map_shared_rank(colk, q)[buf * n + i] = ca[i];
             }
+            if (warp == 0) {
+                float best = -1.f;
+                int bi = k;
+                for (int i = k + lane; i < n; i += 32) {
+                    const float2 v = ca[i];
+                    const float m = v.x * v.x + v.y * v.y;
+                    if (m > best) { best = m; bi = i; }
+                }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            for (int q = 0; q < CL; ++q) {
-                float2* rc = cl.map_shared_rank(colk, q) + buf * n;
-                for (int i = lane; i < n; i += 32) rc[i] = ca[i];
-                if (lane == 0) cl.map_shared_rank(meta, q)[buf] = best > 0.f ? bi : -1;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane < CL) cl.map_shared_rank(meta, lane)[buf] = best > 0.f ? bi : -1;
             }
         }
         cl.sync();
@@ -144,28 +148,28 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gj_k
         const float2 pv = ck[p];
         const float s2 = 1.f / (pv.x * pv.x + pv.y * pv.y);
         const float2 d = make_float2(pv.x * s2, -pv.y * s2);  // 1 / pivot
-        // exchange rows k and p, scale the new row k
-        for (int jl = threadIdx.x; jl < wl; jl += blockDim.x) {
-            float2* col = A + (size_t)jl * n;
-            const float2 vk = col[k], vp = col[p];
-            col[p] = vk;
-            col[k] = c0 + jl == k ? d : cmul(vp, d);
-        }
-        __syncthreads();
-        // eliminate column k from every other row; column k becomes -m_i / pivot
+        // each warp takes whole columns: exchange rows k and p, scale the new
+        // row k, eliminate column k from every other row (column k itself
+        // becomes -m_i / pivot, and its row k 1 / pivot)
         for (int jl = warp; jl < wl; jl += nw) {
             float2* col = A + (size_t)jl * n;
             const bool kcol = c0 + jl == k;
-            const float2 rk = col[k];
+            const float2 vk = col[k], vp = col[p];
+            __syncwarp();
+            const float2 rk = kcol ? d : cmul(vp, d);  // the new row k
             for (int i = lane; i < n; i += 32) {
-                if (i == k) continue;
+                if (i == k) {
+                    col[k] = rk;
+                    continue;
+                }
                 const float2 m = ck[i == p ? k : i];  // a_ik after the exchange
                 if (kcol) {
                     const float2 t = cmul(m, d);
                     col[i] = make_float2(-t.x, -t.y);
                 } else {
+                    const float2 cur = i == p ? vk : col[i];
                     const float2 t = cmul(m, rk);
-                    col[i] = make_float2(col[i].x - t.x, col[i].y - t.y);
+                    col[i] = make_float2(cur.x - t.x, cur.y - t.y);
                 }
             }
         }
@@ -258,6 +262,7 @@ struct DftJob {
 };
 struct DftArgs {
     int n;
+    float2 tw[FT_MAX_SECTORS];  // (cos, sin) of 2 pi k / nth (the kernels specialised on nth read these)
     DftJob j[FT_JOBS];
 };
 
@@ -387,8 +392,165 @@ __global__ void __launch_bounds__(64) idft_kernel(const __grid_constant__ DftArg
     }
 }
 
+// The same transforms and block builder for a sector count known at compile
+// time: every loop over sectors and frequencies unrolled, so the twiddle index
+// (f s mod NTH) is a constant and the twiddles (kernel parameters) are constant
+// operands of the multiply-adds; each CTA of the transforms takes FT_JC columns.
+constexpr int FT_JC = 4;
+
+// One column per CTA: the column of X (3 Nt values) and the tube's panel map are
+// staged in shared memory with coalesced loads first, so the sector loop reads
+// shared memory only (dynamic shared memory: 4 (3 Nt + nb NTH) bytes).
+template <int NTH, class TI>
+__global__ void __launch_bounds__(192, 4) fdft_nth(const __grid_constant__ DftArgs args) {
+    constexpr int NF = NTH / 2 + 1;
+    extern __shared__ float fsm[];
+    const DftJob& J = args.j[blockIdx.y];
+    const int j = blockIdx.x;
+    if (j >= J.nc) return;
+    const int n3 = 3 * J.nb, nt = n3 * NTH;
+    float* xs = fsm;                                   // the column, nt values
+    int* pan = reinterpret_cast<int*>(fsm + nt);       // nb x NTH panel map
+    const TI* x = reinterpret_cast<const TI*>(J.x) + (long long)j * J.ldx;
+    for (int e = threadIdx.x; e < nt; e += blockDim.x) xs[e] = (float)x[e];
+    for (int e = threadIdx.x; e < J.nb * NTH; e += blockDim.x) pan[e] = J.panel[e];
+    __syncthreads();
+    const float scale = 1.f / (float)NTH;
+    for (int r = threadIdx.x; r < n3; r += blockDim.x) {
+        const int a = r / 3, al = r - 3 * a;
+        const int* pa = pan + a * NTH;
+        float re[NF], im[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
+#pragma unroll
+        for (int s = 0; s < NTH; ++s) {
+            const float* xp = xs + 3 * pa[s];
+            float v;  // (R_s^T x_p)_al
+            if (al == 2) v = xp[2];
+            else {
+                const float c = args.tw[s].x, sn = args.tw[s].y;
+                v = al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
+            }
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                re[f] += v * args.tw[(f * s) % NTH].x;
+                im[f] -= v * args.tw[(f * s) % NTH].y;
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const long long o = ((long long)f * J.nc + j) * J.ldk;
+            const float vr = re[f] * scale, vi = im[f] * scale;
+            const bf16 hr = __float2bfloat16_rn(vr), hi = __float2bfloat16_rn(vi);
+            J.h[o + r] = hr;
+            J.l[o + r] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+            J.h[o + n3 + r] = hi;
+            J.l[o + n3 + r] = __float2bfloat16_rn(vi - __bfloat162float(hi));
+        }
+    }
+}
+
+// threadIdx.x: representative (strided), threadIdx.y: one of FT_JC columns
+template <int NTH, class TO>
+__global__ void __launch_bounds__(256) idft_nth(const __grid_constant__ DftArgs args) {
+    constexpr int NF = NTH / 2 + 1;
+    const DftJob& J = args.j[blockIdx.y];
+    const int j = blockIdx.x * FT_JC + threadIdx.y;
+    if (j >= J.nc) return;
+    const int n3 = 3 * J.nb;
+    const float* yh = reinterpret_cast<const float*>(J.x) + (long long)j * J.ldk;
+    const long long plane = (long long)J.nc * J.ldk;
+    TO* y = reinterpret_cast<TO*>(J.y) + (long long)j * J.ldy;
+    for (int a = threadIdx.x; a < J.nb; a += blockDim.x) {
+        const int* pa = J.panel + a * NTH;
+        // pass 0: components 0 and 1 (the rotation mixes them); pass 1: component 2
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            const int nc2 = pass == 0 ? 2 : 1, c0 = pass == 0 ? 0 : 2;
+            float yr[2][NF], yi[2][NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const float wgt = (f == 0 || 2 * f == NTH) ? 1.f : 2.f;
+                const float* pf = yh + f * plane;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    yr[c][f] = c < nc2 ? wgt * pf[3 * a + c0 + c] : 0.f;
+                    yi[c][f] = c < nc2 ? wgt * pf[n3 + 3 * a + c0 + c] : 0.f;
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < NTH; ++s) {
+                float v[2];
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    float t = 0.f;
+#pragma unroll
+                    for (int f = 0; f < NF; ++f)
+                        t += args.tw[(f * s) % NTH].x * yr[c][f] - args.tw[(f * s) % NTH].y * yi[c][f];
+                    v[c] = t;
+                }
+                const float cs = args.tw[s].x, sn = args.tw[s].y;
+                float o[2];
+                long long row;
+                if (pass == 0) {
+                    o[0] = cs * v[0] - sn * v[1];
+                    o[1] = sn * v[0] + cs * v[1];
+                    row = 3LL * pa[s];
+                } else {
+                    o[0] = v[0];
+                    o[1] = 0.f;
+                    row = 3LL * pa[s] + 2;
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    if (q >= nc2) break;
+                    y[row + q] = (TO)o[q];
+                    if (J.h) {
+                        const long long e = row + q + (long long)j * J.lds;
+                        const bf16 h = __float2bfloat16_rn(o[q]);
+                        J.h[e] = h;
+                        J.l[e] = __float2bfloat16_rn(o[q] - __bfloat162float(h));
+                    }
+                }
+            }
+        }
+    }
+}
+
+// C^_f in FP32 for a compile-time sector count (thread: row r; blockIdx.y: column)
+template <int NTH>
+__global__ void chat_nth(const __grid_constant__ ChatArgs args, const __grid_constant__ DftArgs tw) {
+    constexpr int NF = NTH / 2 + 1;
+    const ChatJob& J = args.j[blockIdx.z];
+    const int n3 = 3 * args.nb;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n3) return;
+    const int c = blockIdx.y, b = c / 3, be = c % 3;
+    const int* pb = J.panel + b * NTH;
+    float re[NF], im[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
+#pragma unroll
+    for (int d = 0; d < NTH; ++d) {
+        const float* col = J.T0 + r + (long long)(3 * pb[d]) * n3;
+        const float cs = tw.tw[d].x, sn = tw.tw[d].y;
+        float v;  // (T0 R_d)[r, 3 q + be]
+        if (be == 2) v = col[2LL * n3];
+        else if (be == 0) v = cs * col[0] + sn * col[n3];
+        else v = -sn * col[0] + cs * col[n3];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            re[f] += v * tw.tw[(f * d) % NTH].x;
+            im[f] += v * tw.tw[(f * d) % NTH].y;
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) J.C[(long long)f * n3 * n3 + (long long)c * n3 + r] = make_float2(re[f], im[f]);
+}
+
 int gj_cluster(int n) {
-    // shared memory of one CTA: its columns, two pivot columns and the index arrays
+    // shared memory of one CTA: its columns, two pivot columns and the index
+    // arrays; two CTAs per block where they fit (measured faster than four)
     for (int cl : {2, 4}) {
         const int w = (n + cl - 1) / cl;
         const size_t bytes = (size_t)n * w * sizeof(float2) + 2 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
@@ -449,7 +611,15 @@ void fourier_build(const std::vector<FourierTube*>& fts, const std::vector<const
                 const size_t k = ids[i0 + q];
                 a.j[q] = {T0s[k], fts[k]->panel.get(), C.get() + (i0 + q) * nf * (size_t)n3 * n3};
             }
-            LAUNCH(chat_kernel, dim3(ceil_div(n3, 64), n3, a.n), 64, 0, cx.st, a);
+            const double cby = 4.0 * 9.0 * a.n * nb * (double)nb * nth + 8.0 * a.n * nf * (double)n3 * n3;
+            const dim3 cg3(ceil_div(n3, 64), n3, a.n);
+            DftArgs tw;
+            for (int d = 0; d < nth; ++d)
+                tw.tw[d] = make_float2((float)std::cos(TWO_PI * d / nth), (float)std::sin(TWO_PI * d / nth));
+            if (nth == 24) TIMED_LAUNCH("fourier_inverse", 0.0, cby, chat_nth<24>, cg3, 64, 0, cx.st, a, tw);
+            else if (nth == 30) TIMED_LAUNCH("fourier_inverse", 0.0, cby, chat_nth<30>, cg3, 64, 0, cx.st, a, tw);
+            else if (nth == 36) TIMED_LAUNCH("fourier_inverse", 0.0, cby, chat_nth<36>, cg3, 64, 0, cx.st, a, tw);
+            else TIMED_LAUNCH("fourier_inverse", 0.0, cby, chat_kernel, cg3, 64, 0, cx.st, a);
         }
         const int cl = gj_cluster(n3);
         const size_t smem = gj_smem(n3, cl);
@@ -473,15 +643,18 @@ void fourier_build(const std::vector<FourierTube*>& fts, const std::vector<const
                 r.lo[b] = fts[k]->Al.get() + (size_t)f * fts[k]->m2 * fts[k]->ldk;
                 r.ldk = fts[k]->ldk;
             }
+            // credited: 8 n^3 FP32 flops per complex inversion; bytes: the block read and written
+            const double gfl = 8.0 * g.nblk * (double)n3 * n3 * n3, gby = 16.0 * g.nblk * (double)n3 * n3;
             if (cl == 2) {
                 CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                LAUNCH(gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
+                TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
             } else {
                 CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                LAUNCH(gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
+                TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
             }
             const int t = ceil_div(2 * n3, 32);
-            LAUNCH(realform_kernel, dim3(t, t, g.nblk), dim3(32, 8), 0, cx.st, r);
+            TIMED_LAUNCH("fourier_inverse", 0.0, g.nblk * (8.0 * n3 * n3 + 16.0 * n3 * n3), realform_kernel,
+                         dim3(t, t, g.nblk), dim3(32, 8), 0, cx.st, r);
         }
     }
 }
@@ -524,12 +697,55 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
     };
     int maxnc = 0;
     for (const FourierJob& J : jobs) maxnc = std::max(maxnc, J.nc);
-    for (size_t i0 = 0; i0 < jobs.size(); i0 += FT_JOBS) {
+    // credited bytes of a transform: X (or Y) once, X^ (or Y^) once
+    auto dft_bytes = [&](size_t i0, int n, bool forward) {
+        double b = 0;
+        for (int q = 0; q < n; ++q) {
+            const FourierJob& J = jobs[i0 + q];
+            const double io = (double)J.ft->nt * J.nc * ((forward ? in64 : out64) ? 8.0 : 4.0);
+            const double hat = (double)J.ft->nf * J.ft->m2 * J.nc * (forward ? 4.0 : 4.0);
+            b += io + hat + (!forward && J.yh ? 4.0 * J.ft->nt * J.nc : 0.0);
+        }
+        return b;
+    };
+    // launches of up to FT_JOBS consecutive jobs with the same sector count
+    auto batches = [&]() {
+        std::vector<std::pair<size_t, int>> b;
+        for (size_t i0 = 0; i0 < jobs.size();) {
+            int n = 1;
+            while (i0 + n < jobs.size() && n < FT_JOBS && jobs[i0 + n].ft->nth == jobs[i0].ft->nth) ++n;
+            b.push_back({i0, n});
+            i0 += n;
+        }
+        return b;
+    };
+    auto set_tw = [&](DftArgs& a, int nth) {
+        for (int k = 0; k < nth; ++k)
+            a.tw[k] = make_float2((float)std::cos(TWO_PI * k / nth), (float)std::sin(TWO_PI * k / nth));
+    };
+    for (const auto& bt : batches()) {
+        const size_t i0 = bt.first;
         DftArgs a;
-        a.n = (int)std::min<size_t>(FT_JOBS, jobs.size() - i0);
+        a.n = bt.second;
         for (int q = 0; q < a.n; ++q) a.j[q] = dft_job(i0 + q, true);
-        if (in64) LAUNCH(fdft_kernel<double>, dim3(maxnc, a.n), 192, 0, cx.st, a);
-        else LAUNCH(fdft_kernel<float>, dim3(maxnc, a.n), 192, 0, cx.st, a);
+        const int nth = jobs[i0].ft->nth;
+        set_tw(a, nth);
+        const double by = dft_bytes(i0, a.n, true);
+        const dim3 gs(maxnc, a.n);
+        int nbmax = 0;
+        for (int q = 0; q < a.n; ++q) nbmax = std::max(nbmax, a.j[q].nb);
+        const size_t sm = sizeof(float) * (size_t)nbmax * nth * 4;  // 3 nb nth column values + nb nth map entries
+        if (in64) {
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, double>), gs, 192, sm, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, double>), gs, 192, sm, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<36, double>), gs, 192, sm, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<double>, dim3(maxnc, a.n), 192, 0, cx.st, a);
+        } else {
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, float>), gs, 192, sm, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, float>), gs, 192, sm, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<36, float>), gs, 192, sm, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<float>, dim3(maxnc, a.n), 192, 0, cx.st, a);
+        }
     }
     // one GEMM of order 2 n3 per job and frequency: Y^_f = inv(C^_f) X^_f in real form
     std::vector<TcProblem> P;
@@ -551,12 +767,26 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
         }
     }
     tc_gemm(P, O, cx.err, nullptr, cx.st);
-    for (size_t i0 = 0; i0 < jobs.size(); i0 += FT_JOBS) {
+    for (const auto& bt : batches()) {
+        const size_t i0 = bt.first;
         DftArgs a;
-        a.n = (int)std::min<size_t>(FT_JOBS, jobs.size() - i0);
+        a.n = bt.second;
         for (int q = 0; q < a.n; ++q) a.j[q] = dft_job(i0 + q, false);
-        if (out64) LAUNCH(idft_kernel<double>, dim3(maxnc, a.n), 64, 0, cx.st, a);
-        else LAUNCH(idft_kernel<float>, dim3(maxnc, a.n), 64, 0, cx.st, a);
+        const int nth = jobs[i0].ft->nth;
+        set_tw(a, nth);
+        const double by = dft_bytes(i0, a.n, false);
+        const dim3 gs(ceil_div(maxnc, FT_JC), a.n), bs(64, FT_JC);
+        if (out64) {
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, double>), gs, bs, 0, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, double>), gs, bs, 0, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, double>), gs, bs, 0, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, idft_kernel<double>, dim3(maxnc, a.n), 64, 0, cx.st, a);
+        } else {
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, float>), gs, bs, 0, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, float>), gs, bs, 0, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, float>), gs, bs, 0, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, idft_kernel<float>, dim3(maxnc, a.n), 64, 0, cx.st, a);
+        }
     }
 }
 
