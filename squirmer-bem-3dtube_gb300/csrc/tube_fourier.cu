@@ -106,6 +106,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gj_k
     int* meta = reinterpret_cast<int*>(colk + 2 * n);  // [2]: pivot row per buffer (-1: zero pivot)
     int* piv = meta + 2;                      // n: pivot row of every step
     int* pos = piv + n;                       // n: output column of every stored column
+    float2* mk = reinterpret_cast<float2*>(pos + n);  // n: multipliers of the step (2 + 2 n ints: 8-byte aligned)
     const int c0 = rank * w, wl = max(0, min(w, n - c0));
     float2* C = blk < args.nblk ? args.C[blk] : nullptr;
     if (C)
@@ -148,28 +149,31 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gj_k
         const float2 pv = ck[p];
         const float s2 = 1.f / (pv.x * pv.x + pv.y * pv.y);
         const float2 d = make_float2(pv.x * s2, -pv.y * s2);  // 1 / pivot
-        // each warp takes whole columns: exchange rows k and p, scale the new
-        // row k, eliminate column k from every other row (column k itself
-        // becomes -m_i / pivot, and its row k 1 / pivot)
+        // the multipliers after the exchange, row k's set to zero
+        for (int i = threadIdx.x; i < n; i += blockDim.x) mk[i] = i == k ? make_float2(0.f, 0.f) : ck[i == p ? k : i];
+        // exchange rows k and p and scale the new row k (one lane per column)
+        for (int jl = threadIdx.x; jl < wl; jl += blockDim.x) {
+            float2* col = A + (size_t)jl * n;
+            const float2 vk = col[k], vp = col[p];
+            col[p] = vk;
+            col[k] = c0 + jl == k ? d : cmul(vp, d);
+        }
+        __syncthreads();
+        // eliminate: column j -= m * (row k), row k itself untouched (m_k = 0);
+        // column k of the inverse: -m_i / pivot (row k: 1 / pivot)
         for (int jl = warp; jl < wl; jl += nw) {
             float2* col = A + (size_t)jl * n;
-            const bool kcol = c0 + jl == k;
-            const float2 vk = col[k], vp = col[p];
-            __syncwarp();
-            const float2 rk = kcol ? d : cmul(vp, d);  // the new row k
-            for (int i = lane; i < n; i += 32) {
-                if (i == k) {
-                    col[k] = rk;
-                    continue;
-                }
-                const float2 m = ck[i == p ? k : i];  // a_ik after the exchange
-                if (kcol) {
-                    const float2 t = cmul(m, d);
-                    col[i] = make_float2(-t.x, -t.y);
-                } else {
-                    const float2 cur = i == p ? vk : col[i];
-                    const float2 t = cmul(m, rk);
-                    col[i] = make_float2(cur.x - t.x, cur.y - t.y);
+            if (c0 + jl == k) {
+                for (int i = lane; i < n; i += 32)
+                    if (i != k) {
+                        const float2 t = cmul(mk[i], d);
+                        col[i] = make_float2(-t.x, -t.y);
+                    }
+            } else {
+                const float2 rk = col[k];
+                for (int i = lane; i < n; i += 32) {
+                    const float2 m = mk[i], c = col[i];
+                    col[i] = make_float2(c.x - (m.x * rk.x - m.y * rk.y), c.y - (m.x * rk.y + m.y * rk.x));
                 }
             }
         }
@@ -396,121 +400,141 @@ __global__ void __launch_bounds__(64) idft_kernel(const __grid_constant__ DftArg
 // time: every loop over sectors and frequencies unrolled, so the twiddle index
 // (f s mod NTH) is a constant and the twiddles (kernel parameters) are constant
 // operands of the multiply-adds; each CTA of the transforms takes FT_JC columns.
-constexpr int FT_JC = 4;
+// Persistent CTAs over the columns of X: the tube's panel map is staged in shared
+// memory once, and the columns go through two shared-memory buffers -- the next
+// column's copy (cp.async) runs while the current one is transformed, so the
+// sector loop reads shared memory only.  FP64 input (the refinement's few
+// columns) is staged synchronously.  Dynamic shared memory: nb NTH map entries +
+// 2 x 3 nb NTH column values.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but(int n) {
+    if (n) asm volatile("cp.async.wait_group 1;" ::: "memory");
+    else asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
 
-// One column per CTA: the column of X (3 Nt values) and the tube's panel map are
-// staged in shared memory with coalesced loads first, so the sector loop reads
-// shared memory only (dynamic shared memory: 4 (3 Nt + nb NTH) bytes).
 template <int NTH, class TI>
-__global__ void __launch_bounds__(192, 4) fdft_nth(const __grid_constant__ DftArgs args) {
+__global__ void __launch_bounds__(192, 3) fdft_nth(const __grid_constant__ DftArgs args) {
     constexpr int NF = NTH / 2 + 1;
+    constexpr bool ASYNC = sizeof(TI) == sizeof(float);
     extern __shared__ float fsm[];
     const DftJob& J = args.j[blockIdx.y];
-    const int j = blockIdx.x;
+    int j = blockIdx.x;
     if (j >= J.nc) return;
     const int n3 = 3 * J.nb, nt = n3 * NTH;
-    float* xs = fsm;                                   // the column, nt values
-    int* pan = reinterpret_cast<int*>(fsm + nt);       // nb x NTH panel map
-    const TI* x = reinterpret_cast<const TI*>(J.x) + (long long)j * J.ldx;
-    for (int e = threadIdx.x; e < nt; e += blockDim.x) xs[e] = (float)x[e];
+    int* pan = reinterpret_cast<int*>(fsm);  // nb x NTH panel map
+    float* buf[2] = {fsm + J.nb * NTH, fsm + J.nb * NTH + nt};
+    const TI* X = reinterpret_cast<const TI*>(J.x);
     for (int e = threadIdx.x; e < J.nb * NTH; e += blockDim.x) pan[e] = J.panel[e];
-    __syncthreads();
+    if (ASYNC) {
+        const float* x = reinterpret_cast<const float*>(X) + (long long)j * J.ldx;
+        for (int e = threadIdx.x; e < nt; e += blockDim.x) cp_async4(buf[0] + e, x + e);
+        cp_async_commit();
+    }
     const float scale = 1.f / (float)NTH;
-    for (int r = threadIdx.x; r < n3; r += blockDim.x) {
-        const int a = r / 3, al = r - 3 * a;
-        const int* pa = pan + a * NTH;
-        float re[NF], im[NF];
+    for (int it = 0;; ++it) {
+        float* xs = buf[it & 1];
+        const int jn = j + gridDim.x;
+        if (ASYNC) {
+            if (jn < J.nc) {
+                const float* x = reinterpret_cast<const float*>(X) + (long long)jn * J.ldx;
+                float* nx = buf[(it + 1) & 1];
+                for (int e = threadIdx.x; e < nt; e += blockDim.x) cp_async4(nx + e, x + e);
+                cp_async_commit();
+            }
+            cp_async_wait_all_but(jn < J.nc ? 1 : 0);
+        } else {
+            const TI* x = X + (long long)j * J.ldx;
+            for (int e = threadIdx.x; e < nt; e += blockDim.x) xs[e] = (float)x[e];
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < n3; r += blockDim.x) {
+            const int a = r / 3, al = r - 3 * a;
+            const int* pa = pan + a * NTH;
+            float re[NF], im[NF];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
+            for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
 #pragma unroll
-        for (int s = 0; s < NTH; ++s) {
-            const float* xp = xs + 3 * pa[s];
-            float v;  // (R_s^T x_p)_al
-            if (al == 2) v = xp[2];
-            else {
-                const float c = args.tw[s].x, sn = args.tw[s].y;
-                v = al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
+            for (int s = 0; s < NTH; ++s) {
+                const float* xp = xs + 3 * pa[s];
+                float v;  // (R_s^T x_p)_al
+                if (al == 2) v = xp[2];
+                else {
+                    const float c = args.tw[s].x, sn = args.tw[s].y;
+                    v = al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
+                }
+#pragma unroll
+                for (int f = 0; f < NF; ++f) {
+                    re[f] += v * args.tw[(f * s) % NTH].x;
+                    im[f] -= v * args.tw[(f * s) % NTH].y;
+                }
             }
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
-                re[f] += v * args.tw[(f * s) % NTH].x;
-                im[f] -= v * args.tw[(f * s) % NTH].y;
+                const long long o = ((long long)f * J.nc + j) * J.ldk;
+                const float vr = re[f] * scale, vi = im[f] * scale;
+                const bf16 hr = __float2bfloat16_rn(vr), hi = __float2bfloat16_rn(vi);
+                J.h[o + r] = hr;
+                J.l[o + r] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+                J.h[o + n3 + r] = hi;
+                J.l[o + n3 + r] = __float2bfloat16_rn(vi - __bfloat162float(hi));
             }
         }
-#pragma unroll
-        for (int f = 0; f < NF; ++f) {
-            const long long o = ((long long)f * J.nc + j) * J.ldk;
-            const float vr = re[f] * scale, vi = im[f] * scale;
-            const bf16 hr = __float2bfloat16_rn(vr), hi = __float2bfloat16_rn(vi);
-            J.h[o + r] = hr;
-            J.l[o + r] = __float2bfloat16_rn(vr - __bfloat162float(hr));
-            J.h[o + n3 + r] = hi;
-            J.l[o + n3 + r] = __float2bfloat16_rn(vi - __bfloat162float(hi));
-        }
+        __syncthreads();  // the buffer just read is the next prefetch's target
+        j = jn;
+        if (j >= J.nc) break;
     }
 }
 
-// threadIdx.x: representative (strided), threadIdx.y: one of FT_JC columns
+// Thread per (representative a, component c) of one column: the 2 nf spectrum
+// values of its row in registers, the twiddles constant operands (NTH known at
+// compile time).  The rotation R_s mixes components 0 and 1, which sit on
+// neighbouring lanes: a warp takes 10 representatives on lanes 0 .. 29 (lanes
+// 30, 31 idle), so the pair never straddles two warps.
 template <int NTH, class TO>
-__global__ void __launch_bounds__(256) idft_nth(const __grid_constant__ DftArgs args) {
+__global__ void __launch_bounds__(192) idft_nth(const __grid_constant__ DftArgs args) {
     constexpr int NF = NTH / 2 + 1;
     const DftJob& J = args.j[blockIdx.y];
-    const int j = blockIdx.x * FT_JC + threadIdx.y;
+    const int j = blockIdx.x;
     if (j >= J.nc) return;
     const int n3 = 3 * J.nb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const float* yh = reinterpret_cast<const float*>(J.x) + (long long)j * J.ldk;
     const long long plane = (long long)J.nc * J.ldk;
     TO* y = reinterpret_cast<TO*>(J.y) + (long long)j * J.ldy;
-    for (int a = threadIdx.x; a < J.nb; a += blockDim.x) {
-        const int* pa = J.panel + a * NTH;
-        // pass 0: components 0 and 1 (the rotation mixes them); pass 1: component 2
-#pragma unroll 1
-        for (int pass = 0; pass < 2; ++pass) {
-            const int nc2 = pass == 0 ? 2 : 1, c0 = pass == 0 ? 0 : 2;
-            float yr[2][NF], yi[2][NF];
+    const int c = lane % 3;
+    for (int a0 = 10 * warp; a0 < J.nb; a0 += 10 * nw) {
+        const int a = a0 + lane / 3;
+        const bool act = lane < 30 && a < J.nb;
+        const int r = 3 * a + c;
+        float yr[NF], yi[NF];
 #pragma unroll
-            for (int f = 0; f < NF; ++f) {
-                const float wgt = (f == 0 || 2 * f == NTH) ? 1.f : 2.f;
-                const float* pf = yh + f * plane;
+        for (int f = 0; f < NF; ++f) {
+            const float wgt = (f == 0 || 2 * f == NTH) ? 1.f : 2.f;
+            yr[f] = act ? wgt * yh[f * plane + r] : 0.f;
+            yi[f] = act ? wgt * yh[f * plane + n3 + r] : 0.f;
+        }
+        const int* pa = J.panel + (act ? a : 0) * NTH;
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    yr[c][f] = c < nc2 ? wgt * pf[3 * a + c0 + c] : 0.f;
-                    yi[c][f] = c < nc2 ? wgt * pf[n3 + 3 * a + c0 + c] : 0.f;
-                }
-            }
+        for (int s = 0; s < NTH; ++s) {
+            float v = 0.f;
 #pragma unroll
-            for (int s = 0; s < NTH; ++s) {
-                float v[2];
-#pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    float t = 0.f;
-#pragma unroll
-                    for (int f = 0; f < NF; ++f)
-                        t += args.tw[(f * s) % NTH].x * yr[c][f] - args.tw[(f * s) % NTH].y * yi[c][f];
-                    v[c] = t;
-                }
-                const float cs = args.tw[s].x, sn = args.tw[s].y;
-                float o[2];
-                long long row;
-                if (pass == 0) {
-                    o[0] = cs * v[0] - sn * v[1];
-                    o[1] = sn * v[0] + cs * v[1];
-                    row = 3LL * pa[s];
-                } else {
-                    o[0] = v[0];
-                    o[1] = 0.f;
-                    row = 3LL * pa[s] + 2;
-                }
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    if (q >= nc2) break;
-                    y[row + q] = (TO)o[q];
-                    if (J.h) {
-                        const long long e = row + q + (long long)j * J.lds;
-                        const bf16 h = __float2bfloat16_rn(o[q]);
-                        J.h[e] = h;
-                        J.l[e] = __float2bfloat16_rn(o[q] - __bfloat162float(h));
-                    }
+            for (int f = 0; f < NF; ++f) v += args.tw[(f * s) % NTH].x * yr[f] - args.tw[(f * s) % NTH].y * yi[f];
+            // partner component: c = 0 <-> 1 (c = 2 keeps its own value)
+            const float w = __shfl_sync(0xffffffffu, v, c == 0 ? lane + 1 : (c == 1 ? lane - 1 : lane));
+            const float cs = args.tw[s].x, sn = args.tw[s].y;
+            const float o = c == 0 ? cs * v - sn * w : (c == 1 ? sn * w + cs * v : v);
+            if (act) {
+                const long long row = 3LL * __ldg(pa + s) + c;
+                y[row] = (TO)o;
+                if (J.h) {
+                    const long long e = row + (long long)j * J.lds;
+                    const bf16 h = __float2bfloat16_rn(o);
+                    J.h[e] = h;
+                    J.l[e] = __float2bfloat16_rn(o - __bfloat162float(h));
                 }
             }
         }
@@ -553,7 +577,7 @@ int gj_cluster(int n) {
     // arrays; two CTAs per block where they fit (measured faster than four)
     for (int cl : {2, 4}) {
         const int w = (n + cl - 1) / cl;
-        const size_t bytes = (size_t)n * w * sizeof(float2) + 2 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
+        const size_t bytes = (size_t)n * w * sizeof(float2) + 3 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
         if (bytes <= 220 * 1024) return cl;
     }
     return 0;
@@ -561,7 +585,7 @@ int gj_cluster(int n) {
 
 size_t gj_smem(int n, int cl) {
     const int w = (n + cl - 1) / cl;
-    return (size_t)n * w * sizeof(float2) + 2 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
+    return (size_t)n * w * sizeof(float2) + 3 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
 }
 
 }  // namespace
@@ -731,10 +755,20 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
         const int nth = jobs[i0].ft->nth;
         set_tw(a, nth);
         const double by = dft_bytes(i0, a.n, true);
-        const dim3 gs(maxnc, a.n);
+        // persistent CTAs: about 8 per SM over the launch's jobs
+        const int per_job = std::max(1, std::min(maxnc, ceil_div(8 * 152, a.n)));
+        const dim3 gs(per_job, a.n);
         int nbmax = 0;
         for (int q = 0; q < a.n; ++q) nbmax = std::max(nbmax, a.j[q].nb);
-        const size_t sm = sizeof(float) * (size_t)nbmax * nth * 4;  // 3 nb nth column values + nb nth map entries
+        const size_t sm = sizeof(float) * (size_t)nbmax * nth * 7;  // map + two columns of 3 nb nth values
+        if (sm > 48 * 1024) {
+            if (nth == 24) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nth == 30) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nth == 36) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nth == 24) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nth == 30) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            if (nth == 36) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        }
         if (in64) {
             if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, double>), gs, 192, sm, cx.st, a);
             else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, double>), gs, 192, sm, cx.st, a);
@@ -775,16 +809,17 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
         const int nth = jobs[i0].ft->nth;
         set_tw(a, nth);
         const double by = dft_bytes(i0, a.n, false);
-        const dim3 gs(ceil_div(maxnc, FT_JC), a.n), bs(64, FT_JC);
+        const dim3 gs(maxnc, a.n), bs(192);
+        const size_t sm = 0;
         if (out64) {
-            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, double>), gs, bs, 0, cx.st, a);
-            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, double>), gs, bs, 0, cx.st, a);
-            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, double>), gs, bs, 0, cx.st, a);
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, double>), gs, bs, sm, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, double>), gs, bs, sm, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, double>), gs, bs, sm, cx.st, a);
             else TIMED_LAUNCH("fourier_dft", 0.0, by, idft_kernel<double>, dim3(maxnc, a.n), 64, 0, cx.st, a);
         } else {
-            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, float>), gs, bs, 0, cx.st, a);
-            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, float>), gs, bs, 0, cx.st, a);
-            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, float>), gs, bs, 0, cx.st, a);
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<24, float>), gs, bs, sm, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<30, float>), gs, bs, sm, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (idft_nth<36, float>), gs, bs, sm, cx.st, a);
             else TIMED_LAUNCH("fourier_dft", 0.0, by, idft_kernel<float>, dim3(maxnc, a.n), 64, 0, cx.st, a);
         }
     }
