@@ -339,17 +339,20 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel(BlockJob<TO> job) {
 }
 
 // FP32 view of a source panel for the mixed far field, formed once per block by
-// far_prep_kernel: vertex offsets from the centroid (exact in FP64, rounded
-// once), normal, area, the centroid as an unevaluated sum hi + lo of two
-// floats, and the squared rule thresholds (0.75 h)^2, (1.5 h)^2, (3 h)^2 lowered
-// (thlo) and raised (thhi) by 1e-5.
+// far_prep_kernel: the offsets of the 7 quadrature nodes from the centroid
+// (sum_k l_k (V_k - c), formed in FP64 and rounded once), the node weights of
+// the single layer (w area) and of the double layer (-6 w area), the normal,
+// the centroid as an unevaluated sum hi + lo of two floats, and the squared rule
+// thresholds (0.75 h)^2, (1.5 h)^2, (3 h)^2 lowered (thlo) and raised (thhi) by
+// 1e-5.  Everything here depends on the source panel only, so the pair loop
+// forms a node as (c - x0) + o_q.
 struct __align__(16) FarF {
-    float d[9];
+    float o[21];
+    float ws[7], wd[7];
     float n[3];
-    float area;
     float chi[3], clo[3];
     float thlo[3], thhi[3];
-    float pad[3];
+    float pad[2];
 };
 static_assert(sizeof(FarF) % 16 == 0, "FarF is copied as float4");
 
@@ -369,19 +372,25 @@ __global__ void far_prep_kernel(const PanelRec* __restrict__ src, int nS, const 
     if (k < nS) {
         const PanelRec& P = src[k];
         FarF F;
-        for (int q = 0; q < 9; ++q) F.d[q] = (float)(P.v[q] - P.c[q % 3]);
+        double d[9];
+        for (int q = 0; q < 9; ++q) d[q] = P.v[q] - P.c[q % 3];
+        for (int q = 0; q < 7; ++q) {
+            const QPoint& R = c_rule7[q];
+            for (int x = 0; x < 3; ++x) F.o[3 * q + x] = (float)(R.l0 * d[x] + R.l1 * d[3 + x] + R.l2 * d[6 + x]);
+            F.ws[q] = (float)(R.w * P.area);
+            F.wd[q] = (float)(-6.0 * R.w * P.area);
+        }
         for (int q = 0; q < 3; ++q) {
             F.n[q] = (float)P.n[q];
             split2(P.c[q], F.chi[q], F.clo[q]);
         }
-        F.area = (float)P.area;
         const double h2 = P.h * P.h;
         const double t[3] = {0.5625 * h2, 2.25 * h2, 9.0 * h2};
         for (int q = 0; q < 3; ++q) {
             F.thlo[q] = (float)(t[q] * (1.0 - 1e-5));
             F.thhi[q] = (float)(t[q] * (1.0 + 1e-5));
-            F.pad[q] = 0.f;
         }
+        F.pad[0] = F.pad[1] = 0.f;
         srcf[k] = F;
     }
     if (k < nT)
@@ -397,15 +406,17 @@ __global__ void far_prep_kernel(const PanelRec* __restrict__ src, int nS, const 
 // shared-memory list first (heavy from the front, light from the back) and
 // appended to the global list with one atomic per class at the end of the CTA,
 // so no thread waits on a global atomic inside the pair loop.
-constexpr int FAR_PAIRS = FAR_TGT * FAR_SRC;
-template <class TO>
-__global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, const FarF* __restrict__ srcf,
+// SRC: source panels per CTA (FAR_SRC, or fewer for blocks with few targets,
+// such as the tube's sector-0 rows, so that the grid still fills the GPU).
+template <class TO, int SRC>
+__global__ void __launch_bounds__(FAR_TGT, 8) far_kernel_f32(BlockJob<TO> job, const FarF* __restrict__ srcf,
                                                           const float* __restrict__ tgtf) {
-    __shared__ FarF sf[FAR_SRC];
+    constexpr int FAR_PAIRS = FAR_TGT * SRC;
+    __shared__ FarF sf[SRC];
     __shared__ int2 nl[FAR_PAIRS];
     __shared__ int ncount[2], nbase[2], rcount[5];
-    const int p0 = blockIdx.y * FAR_SRC;
-    const int ns = min(FAR_SRC, job.nS - p0);
+    const int p0 = blockIdx.y * SRC;
+    const int ns = min(SRC, job.nS - p0);
     {
         const float4* s4 = reinterpret_cast<const float4*>(srcf + p0);
         float4* d4 = reinterpret_cast<float4*>(sf);
@@ -425,6 +436,12 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         self_p = job.same_mesh ? i : (job.self_of ? job.self_of[i] : -1);
     }
     const float ss = (float)job.sscale, ds = (float)job.dscale;
+    // column-major outputs (row stride 1, every block of the mixed path): per
+    // target row 3 i the row bases, per pair one column offset
+    const bool colmajor = (!job.S || job.s_rs == 1) && (!job.D || job.d_rs == 1);
+    const long long scs = job.s_cs, dcs = job.d_cs;
+    TO* const Sr = job.S ? job.S + 3LL * i : nullptr;
+    TO* const Dr = job.D ? job.D + 3LL * i : nullptr;
     for (int s = 0; s < nsi; ++s) {
         const FarF& F = sf[s];
         const int p = p0 + s;
@@ -448,14 +465,44 @@ __global__ void __launch_bounds__(FAR_TGT) far_kernel_f32(BlockJob<TO> job, cons
         }
         Acc<float> A;
         A.zero();
-        // r = (c - x0) + sum_k l_k (V_k - c)
+        // r = (c - x0) + o_q; the accumulation of accum<float, true> with the
+        // node weights precomputed
+        const float mx = F.n[0], my = F.n[1], mz = F.n[2];
 #pragma unroll
         for (int q = 0; q < 7; ++q) {
-            const float l0 = c_rule7f[q].l0, l1 = c_rule7f[q].l1, l2 = c_rule7f[q].l2, w = c_rule7f[q].w;
-            const float rx = bx + (l0 * F.d[0] + l1 * F.d[3] + l2 * F.d[6]);
-            const float ry = by + (l0 * F.d[1] + l1 * F.d[4] + l2 * F.d[7]);
-            const float rz = bz + (l0 * F.d[2] + l1 * F.d[5] + l2 * F.d[8]);
-            accum<float, true>(A, rx, ry, rz, w * F.area, F.n[0], F.n[1], F.n[2]);
+            const float rx = bx + F.o[3 * q], ry = by + F.o[3 * q + 1], rz = bz + F.o[3 * q + 2];
+            const float r2 = rx * rx + ry * ry + rz * rz;
+            const float ir = rsqrtf(r2);
+            const float ir2 = ir * ir;
+            const float ir3 = ir * ir2;
+            const float sw = F.ws[q] * ir3;
+            A.dg += F.ws[q] * ir;
+            const float sx = sw * rx, sy = sw * ry, sz = sw * rz;
+            A.sxx += sx * rx; A.sxy += sx * ry; A.sxz += sx * rz;
+            A.syy += sy * ry; A.syz += sy * rz; A.szz += sz * rz;
+            const float dd = (F.wd[q] * ir3) * ((rx * mx + ry * my + rz * mz) * ir2);
+            const float dx = dd * rx, dy = dd * ry, dz = dd * rz;
+            A.dxx += dx * rx; A.dxy += dx * ry; A.dxz += dx * rz;
+            A.dyy += dy * ry; A.dyz += dy * rz; A.dzz += dz * rz;
+        }
+        if (colmajor) {
+            // the 3x3 block at base + 3 p ld + a + b ld: one base per pair, the
+            // columns b = 1, 2 at the hoisted strides, rows a as immediates
+            if (Sr) {
+                TO* sp = Sr + 3LL * p * scs;
+#pragma unroll
+                for (int b = 0; b < 3; ++b)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) sp[a + b * scs] = (TO)(sl_entry(A, a, b) * ss);
+            }
+            if (Dr) {
+                TO* dp = Dr + 3LL * p * dcs;
+#pragma unroll
+                for (int b = 0; b < 3; ++b)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) dp[a + b * dcs] = (TO)(dl_entry(A, a, b) * ds);
+            }
+            continue;
         }
 #pragma unroll
         for (int b = 0; b < 3; ++b)
@@ -561,6 +608,9 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
         job.rule_count = rc.get();
     }
     dim3 grid(ceil_div(job.nT, FAR_TGT), ceil_div(job.nS, FAR_SRC));
+    // few target blocks (the tube's sector-0 rows): 4 sources per CTA, 4x the CTAs
+    const bool narrow = mixed && (long long)grid.x * grid.y < 2LL * 152 * 4;
+    const dim3 grid4(grid.x, ceil_div(job.nS, 4));
     // credited work: every pair considered, at the 7-point rule; bytes written
     const double pairs = (double)job.nT * job.nS;
     const double fl = pairs * 7.0 * FLOPS_PER_EVAL;
@@ -570,7 +620,11 @@ void assemble_block(const BlockJob<TO>& job0, int near_cap, cudaStream_t st, boo
         DevBuf<float> tgtf((size_t)job.nT * 6, st);
         LAUNCH(far_prep_kernel, ceil_div(std::max(job.nS, job.nT), 128), 128, 0, st, job.src, job.nS, job.tgt, job.nT,
                srcf.get(), tgtf.get());
-        TIMED_LAUNCH("assemble_far", fl, by, far_kernel_f32<TO>, grid, FAR_TGT, 0, st, job, srcf.get(), tgtf.get());
+        if (narrow)
+            TIMED_LAUNCH("assemble_far", fl, by, (far_kernel_f32<TO, 4>), grid4, FAR_TGT, 0, st, job, srcf.get(), tgtf.get());
+        else
+            TIMED_LAUNCH("assemble_far", fl, by, (far_kernel_f32<TO, FAR_SRC>), grid, FAR_TGT, 0, st, job, srcf.get(),
+                         tgtf.get());
     } else {
         TIMED_LAUNCH("assemble_far", fl, by, far_kernel<TO>, grid, FAR_TGT, 0, st, job);
     }

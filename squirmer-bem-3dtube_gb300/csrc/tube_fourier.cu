@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -588,6 +589,27 @@ size_t gj_smem(int n, int cl) {
     return (size_t)n * w * sizeof(float2) + 3 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
 }
 
+// The dynamic shared memory limits of the kernels that need more than 48 KB, set
+// once per process to the largest size any launch asks for: concurrent host
+// threads launch blocks of different orders, and a per-launch setting could
+// lower the limit between another thread's setting and its launch.
+constexpr int FT_SMEM_MAX = 220 * 1024;
+void set_smem_limits() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
+        CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
+        // the forward transform: the panel map and two columns, 7 nb n_theta floats (<= 7 * 256 / 3 * 36 * 4 B)
+        const int fd = 7 * (FT_MAX_ORDER / 3) * FT_MAX_SECTORS * 4;
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
+    });
+}
+
 }  // namespace
 
 bool fourier_supported(const TubeSymmetry& sym) {
@@ -669,13 +691,9 @@ void fourier_build(const std::vector<FourierTube*>& fts, const std::vector<const
             }
             // credited: 8 n^3 FP32 flops per complex inversion; bytes: the block read and written
             const double gfl = 8.0 * g.nblk * (double)n3 * n3 * n3, gby = 16.0 * g.nblk * (double)n3 * n3;
-            if (cl == 2) {
-                CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
-            } else {
-                CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
-            }
+            set_smem_limits();
+            if (cl == 2) TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
+            else TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
             const int t = ceil_div(2 * n3, 32);
             TIMED_LAUNCH("fourier_inverse", 0.0, g.nblk * (8.0 * n3 * n3 + 16.0 * n3 * n3), realform_kernel,
                          dim3(t, t, g.nblk), dim3(32, 8), 0, cx.st, r);
@@ -761,14 +779,7 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
         int nbmax = 0;
         for (int q = 0; q < a.n; ++q) nbmax = std::max(nbmax, a.j[q].nb);
         const size_t sm = sizeof(float) * (size_t)nbmax * nth * 7;  // map + two columns of 3 nb nth values
-        if (sm > 48 * 1024) {
-            if (nth == 24) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nth == 30) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nth == 36) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nth == 24) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nth == 30) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            if (nth == 36) CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        }
+        set_smem_limits();
         if (in64) {
             if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, double>), gs, 192, sm, cx.st, a);
             else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, double>), gs, 192, sm, cx.st, a);
