@@ -210,14 +210,17 @@ int group_max() {
 
 // Host wall time per phase of the grouped mixed path, printed to stderr when
 // SQBEM_HOST_TIMING is set (profiling aid).
+// Each line: the phase's duration and the time since the batch call began.
 struct PhaseClock {
     bool on = std::getenv("SQBEM_HOST_TIMING") != nullptr;
     std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    std::chrono::steady_clock::time_point t0 = t;
     void lap(const char* what, size_t G, int ntp, int ns) {
         if (!on) return;
         const auto now = std::chrono::steady_clock::now();
-        std::fprintf(stderr, "host %-14s G=%zu ntp=%d Ns=%d %.2f ms\n", what, G, ntp, ns,
-                     std::chrono::duration<double, std::milli>(now - t).count());
+        std::fprintf(stderr, "host %-14s G=%zu ntp=%d Ns=%d %.2f ms (at %.2f ms)\n", what, G, ntp, ns,
+                     std::chrono::duration<double, std::milli>(now - t).count(),
+                     std::chrono::duration<double, std::milli>(now - t0).count());
         t = now;
     }
 };
@@ -394,8 +397,10 @@ void run_mixed(int n, const sqbem_instance* inst, const std::vector<Prepared>& p
         const double xc[3] = {P.b, 0, 0};
         shares[c.ns] = build_sphere_blocks(make_panels(P.sphereV.data(), P.sphere.P()), xc, 1.0, bs);
     }
+    const auto call_start = std::chrono::steady_clock::now();
     run_concurrent(chunks.size(), bytes, bs, [&](size_t k, cudaStream_t st) {
         PhaseClock pc;
+        pc.t0 = call_start;
         run_chunk(chunks[k].ids, chunks[k].ntp, chunks[k].ns, inst, prep, st, out, pc, shares[chunks[k].ns]);
     });
 }
