@@ -519,11 +519,20 @@ __global__ void __launch_bounds__(192) idft_nth(const __grid_constant__ DftArgs 
             yi[f] = act ? wgt * yh[f * plane + n3 + r] : 0.f;
         }
         const int* pa = J.panel + (act ? a : 0) * NTH;
-#pragma unroll
+        // the sector loop rolled: the twiddle index f s mod NTH is the same on
+        // every lane, so the twiddles are broadcast constant-cache loads, and the
+        // thread holds only its 2 NF spectrum values
+#pragma unroll 1
         for (int s = 0; s < NTH; ++s) {
             float v = 0.f;
+            int k = 0;
 #pragma unroll
-            for (int f = 0; f < NF; ++f) v += args.tw[(f * s) % NTH].x * yr[f] - args.tw[(f * s) % NTH].y * yi[f];
+            for (int f = 0; f < NF; ++f) {
+                const float2 t = args.tw[k];
+                v += t.x * yr[f] - t.y * yi[f];
+                k += s;
+                if (k >= NTH) k -= NTH;
+            }
             // partner component: c = 0 <-> 1 (c = 2 keeps its own value)
             const float w = __shfl_sync(0xffffffffu, v, c == 0 ? lane + 1 : (c == 1 ? lane - 1 : lane));
             const float cs = args.tw[s].x, sn = args.tw[s].y;
