@@ -458,20 +458,34 @@ __global__ void __launch_bounds__(192, 3) fdft_nth(const __grid_constant__ DftAr
             float re[NF], im[NF];
 #pragma unroll
             for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
-#pragma unroll
-            for (int s = 0; s < NTH; ++s) {
+            // (R_s^T x_p)_al of sector s
+            auto vsec = [&](int s) {
                 const float* xp = xs + 3 * pa[s];
-                float v;  // (R_s^T x_p)_al
-                if (al == 2) v = xp[2];
-                else {
-                    const float c = args.tw[s].x, sn = args.tw[s].y;
-                    v = al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
-                }
+                if (al == 2) return xp[2];
+                const float c = args.tw[s].x, sn = args.tw[s].y;
+                return al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
+            };
+            // real input: sectors s and NTH - s share cos(2 pi f s / NTH) and have
+            // opposite sines, so they enter as their sum and difference
+            {
+                const float v0 = vsec(0);
+#pragma unroll
+                for (int f = 0; f < NF; ++f) re[f] = v0;
+            }
+#pragma unroll
+            for (int s = 1; 2 * s < NTH; ++s) {
+                const float va = vsec(s), vb = vsec(NTH - s);
+                const float sum = va + vb, dif = va - vb;
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
-                    re[f] += v * args.tw[(f * s) % NTH].x;
-                    im[f] -= v * args.tw[(f * s) % NTH].y;
+                    re[f] += sum * args.tw[(f * s) % NTH].x;
+                    im[f] -= dif * args.tw[(f * s) % NTH].y;
                 }
+            }
+            if ((NTH & 1) == 0) {  // sector NTH / 2: w^{-f NTH/2} = (-1)^f
+                const float vh = vsec(NTH / 2);
+#pragma unroll
+                for (int f = 0; f < NF; ++f) re[f] += (f & 1) ? -vh : vh;
             }
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
@@ -522,17 +536,9 @@ __global__ void __launch_bounds__(192) idft_nth(const __grid_constant__ DftArgs 
         // the sector loop rolled: the twiddle index f s mod NTH is the same on
         // every lane, so the twiddles are broadcast constant-cache loads, and the
         // thread holds only its 2 NF spectrum values
-#pragma unroll 1
-        for (int s = 0; s < NTH; ++s) {
-            float v = 0.f;
-            int k = 0;
-#pragma unroll
-            for (int f = 0; f < NF; ++f) {
-                const float2 t = args.tw[k];
-                v += t.x * yr[f] - t.y * yi[f];
-                k += s;
-                if (k >= NTH) k -= NTH;
-            }
+        // y~_s = A_s - B_s and y~_{NTH-s} = A_s + B_s with A_s = sum_f cos(2 pi f s / NTH) y^r_f and
+        // B_s = sum_f sin(2 pi f s / NTH) y^i_f: the two sectors from one pair of sums
+        auto emit = [&](int s, float v) {
             // partner component: c = 0 <-> 1 (c = 2 keeps its own value)
             const float w = __shfl_sync(0xffffffffu, v, c == 0 ? lane + 1 : (c == 1 ? lane - 1 : lane));
             const float cs = args.tw[s].x, sn = args.tw[s].y;
@@ -547,6 +553,21 @@ __global__ void __launch_bounds__(192) idft_nth(const __grid_constant__ DftArgs 
                     J.l[e] = __float2bfloat16_rn(o - __bfloat162float(h));
                 }
             }
+        };
+#pragma unroll 1
+        for (int s = 0; 2 * s <= NTH; ++s) {
+            float A = 0.f, B = 0.f;
+            int k = 0;
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                const float2 t = args.tw[k];
+                A += t.x * yr[f];
+                B += t.y * yi[f];
+                k += s;
+                if (k >= NTH) k -= NTH;
+            }
+            emit(s, A - B);
+            if (s > 0 && 2 * s < NTH) emit(NTH - s, A + B);
         }
     }
 }
