@@ -6,12 +6,16 @@
 // fresh pages while the GPU waits.  sqbem_trim_pool() gives the cached memory
 // back.
 //
-// Host-to-device copies of more than a few kilobytes from pageable memory can
-// wait for the stream to drain; they go through pinned staging blocks instead
-// (copied on the host, then a truly asynchronous DMA).  A block is reused once
-// the event recorded after its copy has completed.
+// A host-to-device copy from pageable memory may wait for its stream to drain
+// before it starts, which stalls the host thread that feeds that stream behind
+// every kernel already queued.  Every upload therefore goes through pinned
+// staging (copied on the host, then a truly asynchronous DMA): copies of up to
+// 64 KB through a ring of fixed 64 KB slots, larger ones through blocks sized
+// for them.  A slot or block is reused once the event recorded after its copy
+// has completed.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -39,8 +43,46 @@ struct Pinned {
 std::mutex g_pin_mu;
 std::deque<Pinned> g_pinned;  // deque: references stay valid as it grows
 size_t g_pinned_total = 0;
-constexpr size_t PINNED_CAP = 1ull << 30;      // at most 1 GiB of staging
-constexpr size_t INLINE_BYTES = 64 * 1024;      // small copies stay direct
+constexpr size_t PINNED_CAP = 1ull << 30;      // at most 1 GiB of block staging
+constexpr size_t SLOT_BYTES = 64 * 1024;        // copies up to this size take a ring slot
+constexpr int SLOTS = 512;                      // 32 MiB of slots
+
+// The ring: slots handed out in turn.  A slot's mutex is held while it is filled
+// and its copy enqueued; a thread that comes round to a slot whose previous copy
+// has not yet completed waits for that copy's event (with 512 slots, only when
+// hundreds of small copies are queued behind long kernels).
+struct Slot {
+    std::mutex mu;
+    cudaEvent_t ev = nullptr;
+    bool used = false;
+};
+std::once_flag g_ring_once;
+char* g_ring = nullptr;  // SLOTS x SLOT_BYTES pinned, or null if that allocation failed
+Slot g_slots[SLOTS];
+std::atomic<unsigned> g_ring_next{0};
+
+bool upload_small(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    std::call_once(g_ring_once, [] {
+        void* p = nullptr;
+        if (cudaMallocHost(&p, (size_t)SLOTS * SLOT_BYTES) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return;
+        }
+        for (Slot& sl : g_slots) CUDA_CHECK(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+        g_ring = static_cast<char*>(p);
+    });
+    if (!g_ring) return false;
+    const unsigned i = g_ring_next.fetch_add(1, std::memory_order_relaxed) % SLOTS;
+    Slot& sl = g_slots[i];
+    std::lock_guard<std::mutex> lk(sl.mu);
+    if (sl.used) CUDA_CHECK(cudaEventSynchronize(sl.ev));
+    char* buf = g_ring + (size_t)i * SLOT_BYTES;
+    std::memcpy(buf, src, bytes);
+    CUDA_CHECK(cudaMemcpyAsync(dst, buf, bytes, cudaMemcpyHostToDevice, st));
+    CUDA_CHECK(cudaEventRecord(sl.ev, st));
+    sl.used = true;
+    return true;
+}
 
 }  // namespace
 
@@ -62,8 +104,10 @@ cudaMemPool_t device_pool() {
 
 void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st) {
     count_h2d(bytes);
-    if (bytes <= INLINE_BYTES) {
-        CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    if (bytes == 0) return;
+    if (bytes <= SLOT_BYTES) {
+        if (!upload_small(dst, src, bytes, st))  // no pinned ring: the plain copy is still correct
+            CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
         return;
     }
     Pinned* blk = nullptr;

@@ -238,6 +238,28 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
         }
         fourier_build(fts, sp, t0p, cx);
         check_ctx(cx, "mixed tube (Fourier blocks)");
+        if (explicit_inverse) {
+            // a tube shared by many swimmers: T^{-1} by solving the identity through
+            // the blocks, FP32 (for the refinement's products) and split row-major
+            // (the left operand of every swimmer's Y = T^{-1} [B | Ct])
+            for (size_t k = 0; k < G; ++k) {
+                MixedTube& M = tubes[k]->mt;
+                const size_t nn = (size_t)M.ntp * M.ntp;
+                M.Ti.alloc(nn, cx.st);
+                M.TiRh.alloc(nn, cx.st);
+                M.TiRl.alloc(nn, cx.st);
+                DevBuf<float> I((size_t)M.nt * M.nt, cx.st);
+                I.zero();
+                pad_identity(I.get(), M.nt, 0, M.nt, cx.st);
+                FourierJob j;
+                j.ft = M.ft.get();
+                j.x32 = I.get(); j.ldx = M.nt; j.nc = M.nt;
+                j.y32 = M.Ti.get(); j.ldy = M.ntp;
+                j.yh = M.TiRh.get(); j.yl = M.TiRl.get(); j.srs = M.ntp; j.scs = 1;
+                fourier_solve({j}, cx);
+            }
+            check_ctx(cx, "mixed tube inverse (Fourier blocks)");
+        }
         return;
     }
     std::vector<MixedLU> lu(G);
@@ -421,7 +443,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             if (sw[k]->tube->mt.fourier() != sw[0]->tube->mt.fourier() ||
                 sw[k]->tube->mt.explicit_inverse() != sw[0]->tube->mt.explicit_inverse())
                 fail(SQBEM_ERR_ARG, "mixed swimmers of one group share a tube mode");
-        if (sw[0]->tube->mt.fourier()) {
+        if (sw[0]->tube->mt.fourier() && !sw[0]->tube->mt.explicit_inverse()) {
             // through the Fourier blocks; Y in its own buffer (ld nt), the split copy
             // in (yh, yl) with ld ntp
             std::vector<FourierJob> fj;
@@ -435,7 +457,7 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
                 a.ft = Tt.ft.get();
                 a.x32 = M.B.get(); a.ldx = M.nt; a.nc = M.ns;
                 a.y32 = M.Y.get(); a.ldy = M.nt;
-                a.yh = yh[k].get(); a.yl = yl[k].get(); a.lds = ntp;
+                a.yh = yh[k].get(); a.yl = yl[k].get(); a.srs = 1; a.scs = ntp;
                 fj.push_back(a);
                 FourierJob b = a;
                 b.x32 = M.Ct.get(); b.nc = 6;

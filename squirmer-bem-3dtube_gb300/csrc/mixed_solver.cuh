@@ -52,7 +52,10 @@ struct MixedTube {
     // per frequency and the inverse transform, for one swimmer or many
     std::unique_ptr<FourierTube> ft;
     bool fourier() const { return ft != nullptr; }
-    bool explicit_inverse() const { return !lu && !ft; }
+    // T^{-1} formed explicitly (a tube shared by many swimmers, also with Fourier
+    // blocks: Y = T^{-1} [B | Ct] is then one large-K GEMM per swimmer, and the
+    // refinement's T^{-1} r still goes through the blocks)
+    bool explicit_inverse() const { return Ti.get() != nullptr; }
 };
 
 struct MixedSwimmer {

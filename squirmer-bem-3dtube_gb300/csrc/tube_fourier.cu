@@ -260,9 +260,9 @@ struct DftJob {
     long long ldx;
     void* y;        // forward: unused; inverse: output Y
     long long ldy;
-    bf16* h;        // forward: X^ split; inverse: optional split copy of Y
-    bf16* l;
-    long long lds;
+    bf16* h;        // forward: X^ split; inverse: optional split copy of Y, element
+    bf16* l;        // (r, j) at r * hrs + j * hcs
+    long long hrs, hcs;
     int nc, nb, nth, nf, ldk;
 };
 struct DftArgs {
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(64) idft_kernel(const __grid_constant__ DftArg
             for (int q = 0; q < nout; ++q) {
                 y[row + q] = (TO)o[q];
                 if (J.h) {
-                    const long long e = row + q + (long long)j * J.lds;
+                    const long long e = (row + q) * J.hrs + (long long)j * J.hcs;
                     const bf16 h = __float2bfloat16_rn(o[q]);
                     J.h[e] = h;
                     J.l[e] = __float2bfloat16_rn(o[q] - __bfloat162float(h));
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(192) idft_nth(const __grid_constant__ DftArgs 
                 const long long row = 3LL * __ldg(pa + s) + c;
                 y[row] = (TO)o;
                 if (J.h) {
-                    const long long e = row + (long long)j * J.lds;
+                    const long long e = row * J.hrs + (long long)j * J.hcs;
                     const bf16 h = __float2bfloat16_rn(o);
                     J.h[e] = h;
                     J.l[e] = __float2bfloat16_rn(o - __bfloat162float(h));
@@ -758,12 +758,12 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
             d.x = in64 ? (const void*)J.x64 : (const void*)J.x32;
             d.ldx = J.ldx;
             d.y = nullptr; d.ldy = 0;
-            d.h = xh[k].get(); d.l = xl[k].get(); d.lds = 0;
+            d.h = xh[k].get(); d.l = xl[k].get(); d.hrs = 1; d.hcs = 0;
         } else {
             d.x = yh[k].get(); d.ldx = 0;
             d.y = out64 ? (void*)J.y64 : (void*)J.y32;
             d.ldy = J.ldy;
-            d.h = J.yh; d.l = J.yl; d.lds = J.lds;
+            d.h = J.yh; d.l = J.yl; d.hrs = J.srs; d.hcs = J.scs;
         }
         return d;
     };

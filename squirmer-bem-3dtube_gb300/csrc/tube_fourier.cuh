@@ -50,7 +50,8 @@ void fourier_build(const std::vector<FourierTube*>& ft, const std::vector<const 
                    const std::vector<const float*>& T0, const MixedCtx& cx);
 
 // Y = T^{-1} X for one tube: X (3 Nt x nc, column-major, leading dimension ldx)
-// in FP32 or FP64, Y likewise, and optionally a split column-major copy of Y.
+// in FP32 or FP64, Y likewise, and optionally a split copy of Y with any row and
+// column strides (column-major for a right operand, row-major for a left one).
 struct FourierJob {
     const FourierTube* ft = nullptr;
     const float* x32 = nullptr;
@@ -60,9 +61,9 @@ struct FourierJob {
     float* y32 = nullptr;
     double* y64 = nullptr;
     long long ldy = 0;
-    bf16* yh = nullptr;
+    bf16* yh = nullptr;           // split copy: element (r, j) at r * srs + j * scs
     bf16* yl = nullptr;
-    long long lds = 0;
+    long long srs = 1, scs = 0;
 };
 // Every job of one call: the same input and output precisions.
 void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx);
