@@ -89,7 +89,10 @@ void DevPanels::set(const std::vector<PanelRec>& host, cudaStream_t st) {
     for (int p = 0; p < P; ++p) area_max = std::max(area_max, 5.0 * host[p].area);
 }
 
-Stream::Stream() { CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+cudaStream_t Stream::get() const {
+    if (owned) std::call_once(once, [this] { CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); });
+    return s;
+}
 Stream::~Stream() {
     if (s && owned) cudaStreamDestroy(s);
 }

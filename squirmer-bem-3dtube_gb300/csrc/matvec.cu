@@ -79,8 +79,10 @@ template <int R, bool PLAIN>
 __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ MvArgs args,
                                                         double* __restrict__ part) {
     constexpr int NB = PLAIN ? 2 * MV_BATCH : MV_BATCH;
-    static_assert(MV_CHUNK % NB == 0, "matvec chunk must be a multiple of the load batch");
-    __shared__ float xs[R][PLAIN ? 1 : 2][MV_CHUNK];
+    static_assert(MV_CHUNK % NB == 0 && NB % 4 == 0, "matvec chunk must be a multiple of the load batch");
+    // the staged vector: xh by column, then (compensated) xl; PLAIN reads four
+    // columns per shared-memory load
+    __shared__ __align__(16) float xs[R][(PLAIN ? 1 : 2) * MV_CHUNK];
     const int jb = blockIdx.z, c = blockIdx.y;
     const int nchunk = args.j[jb].nchunk;
     if (c >= nchunk) return;
@@ -95,8 +97,8 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
         const int k = e / MV_CHUNK, j = e % MV_CHUNK;
         const double v = (k < r && j < nj) ? X[j0 + j + (long long)k * ldx] : 0.0;
         const float h = (float)v;
-        xs[k][0][j] = h;
-        if (!PLAIN) xs[k][PLAIN ? 0 : 1][j] = (float)(v - (double)h);
+        xs[k][j] = h;
+        if (!PLAIN) xs[k][MV_CHUNK + j] = (float)(v - (double)h);
     }
     __syncthreads();
     const int row = blockIdx.x * MV_ROWS + threadIdx.x;
@@ -111,13 +113,23 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
         float av[NB];
 #pragma unroll
         for (int u = 0; u < NB; ++u) av[u] = j + u < nj ? __ldg(a + (long long)(j + u) * lda) : 0.f;
+        if (PLAIN) {
 #pragma unroll
-        for (int u = 0; u < NB; ++u)
+            for (int u = 0; u < NB; u += 4)
 #pragma unroll
-            for (int k = 0; k < R; ++k) {
-                if (PLAIN) s[k] = fmaf(av[u], xs[k][0][j + u], s[k]);
-                else dot2_step(s[k], cc[k], av[u], xs[k][0][j + u], xs[k][PLAIN ? 0 : 1][j + u]);
-            }
+                for (int k = 0; k < R; ++k) {
+                    const float4 q = *reinterpret_cast<const float4*>(&xs[k][j + u]);
+                    s[k] = fmaf(av[u], q.x, s[k]);
+                    s[k] = fmaf(av[u + 1], q.y, s[k]);
+                    s[k] = fmaf(av[u + 2], q.z, s[k]);
+                    s[k] = fmaf(av[u + 3], q.w, s[k]);
+                }
+        } else {
+#pragma unroll
+            for (int u = 0; u < NB; ++u)
+#pragma unroll
+                for (int k = 0; k < R; ++k) dot2_step(s[k], cc[k], av[u], xs[k][j + u], xs[k][MV_CHUNK + j + u]);
+        }
     }
     double* o = part + poff + ((long long)c * m + row) * rstride;
 #pragma unroll
@@ -160,6 +172,62 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial(const __grid_constant__ Mv
 #pragma unroll
     for (int k = 0; k < R; ++k)
         if (k < r) o[k] = s[k];
+}
+
+// Jobs with few rows (the six constraint rows F against the sphere unknowns):
+// one thread per row would leave each CTA a handful of threads walking MV_CHUNK
+// dependent loads.  Here a warp takes a row and MV_WIDE columns, its lanes
+// interleaved over the columns, and a shuffle tree adds the lanes' sums (a
+// fixed order, so the result does not depend on scheduling).  FP64 products
+// and sums whatever the matrix's precision: the work is a few kilobytes.
+constexpr int MV_FEW = 32;    // rows at most
+constexpr int MV_WIDE = 256;  // columns per CTA: 8 per lane, loaded together
+constexpr int MV_FEW_WARPS = 8;
+template <int R>
+__global__ void __launch_bounds__(32 * MV_FEW_WARPS) mv_few(const __grid_constant__ MvArgs args,
+                                                           double* __restrict__ part) {
+    const MvDev& D = args.j[blockIdx.z];
+    const MvJob& J = D.j;
+    const int c = blockIdx.y;
+    if (c >= D.nchunk) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int j0 = c * MV_WIDE, j1 = min(J.n, j0 + MV_WIDE);
+    const int r = J.r;
+    for (int row = w; row < J.m; row += MV_FEW_WARPS) {  // warp-uniform
+        double s[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) s[k] = 0.0;
+        constexpr int PER = MV_WIDE / 32;
+        double v[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int j = j0 + lane + 32 * u;
+            const long long o = row + (long long)j * J.lda;
+            v[u] = j < j1 ? (J.A32 ? (double)__ldg(J.A32 + o) : __ldg(J.A64 + o)) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (k >= r) break;
+            double xv[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int j = j0 + lane + 32 * u;
+                xv[u] = j < j1 ? __ldg(J.x + j + (long long)k * J.ldx) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < PER; ++u) s[k] = fma(v[u], xv[u], s[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], d);
+        if (lane == 0) {
+            double* o = part + D.part_off + ((long long)c * J.m + row) * D.rstride;
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+                if (k < r) o[k] = s[k];
+        }
+    }
 }
 
 __global__ void mv_finish(const __grid_constant__ MvArgs args, const double* __restrict__ part) {
@@ -336,10 +404,12 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
         long long off = 0;
         int maxm = 0, maxc = 0, maxr = 0;
         double bytes = 0;
+        bool few = true;
+        for (int k = 0; k < a.n; ++k) few = few && jobs[i0 + k].m <= MV_FEW;
         for (int k = 0; k < a.n; ++k) {
             const MvJob& j = jobs[i0 + k];
             a.j[k].j = j;
-            a.j[k].nchunk = std::max(1, ceil_div(j.n, MV_CHUNK));
+            a.j[k].nchunk = std::max(1, ceil_div(j.n, few ? MV_WIDE : MV_CHUNK));
             a.j[k].part_off = off;
             a.j[k].rstride = j.r;
             off += (long long)a.j[k].nchunk * j.m * j.r;
@@ -354,12 +424,16 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
         for (int k = 0; k < a.n; ++k) all32 = all32 && a.j[k].j.A32 != nullptr;
         if (kstats_on()) {
             char note[96];
-            std::snprintf(note, sizeof note, "jobs=%d m=%d chunks=%d r=%d fp32=%d plain=%d", a.n, maxm, maxc, maxr,
-                          (int)all32, (int)(all32 && a.j[0].j.plain));
+            std::snprintf(note, sizeof note, "jobs=%d m=%d chunks=%d r=%d fp32=%d plain=%d few=%d", a.n, maxm, maxc,
+                          maxr, (int)all32, (int)(all32 && a.j[0].j.plain), (int)few);
             kstat_note(note);
         }
         const bool plain = all32 && a.j[0].j.plain;
-        if (plain) {
+        if (few) {
+            const dim3 g(1, maxc, (unsigned)a.n);
+            if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_few<2>, g, 32 * MV_FEW_WARPS, 0, st, a, part.get());
+            else TIMED_LAUNCH("matvec", 0.0, bytes, mv_few<MV_RMAX>, g, 32 * MV_FEW_WARPS, 0, st, a, part.get());
+        } else if (plain) {
             if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<2, true>), grid, MV_ROWS, 0, st, a, part.get());
             else TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<MV_RMAX, true>), grid, MV_ROWS, 0, st, a, part.get());
         } else if (all32) {

@@ -10,7 +10,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -322,6 +324,16 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
     if (sw.empty()) return;
     const size_t G = sw.size();
     const bool bounded = sw[0]->tube != nullptr;
+    // host time per phase on stderr when SQBEM_HOST_TIMING is set (profiling aid)
+    static const bool timing = std::getenv("SQBEM_HOST_TIMING") != nullptr;
+    auto tp = std::chrono::steady_clock::now();
+    auto lap = [&](const char* what) {
+        if (!timing) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "  swimmers G=%zu %-10s %.2f ms\n", G, what,
+                     std::chrono::duration<double, std::milli>(now - tp).count());
+        tp = now;
+    };
     std::vector<CopyJob> cj;
     std::vector<MvJob> mj;
     std::vector<RigidJob> rj;
@@ -391,12 +403,14 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         M.F.alloc(F.size(), cx.st);
         M.F.upload(F.data(), F.size());
     }
+    lap("members");
     matvec_group(mj, cx.st);
     rigid_product_group(rj, cx.st);
     copy_group(cj, cx.st);
     cj.clear();
     mj.clear();
     tmp.clear();
+    lap("rigid");
 
     // G = [E | Cs] (- D Y with Y = T^{-1} [B | Ct] when bounded), G_s padded
     std::vector<MixedLU> glu(G);
@@ -435,7 +449,9 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             }
             conv.push_back({M.D.get(), 1, M.ns, M.ns, M.nt, dh[k].get(), dl[k].get(), ntp, 1});
         }
+        lap("G setup");
         convert_group(conv, cx.st);
+        lap("convert");
         // Y = T^{-1} [B | Ct]   (FP32 for the refinement, split for the Schur product)
         std::vector<TcProblem> P;
         std::vector<TcOperands> O;
@@ -535,9 +551,12 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
             O.push_back(o2);
         }
         tc_gemm(P, O, cx.err, nullptr, cx.st);
+        lap("Y, D Y");
     }
     mixed_lu_factor(gl, cx);
+    lap("LU");
     check_ctx(cx, "dgetrf (mixed Schur factor)");
+    lap("LU wait");
     // keep G_s's factor (the solves read only the split factor and the block
     // inverses); Z = G_s^{-1} G_c by block substitutions, then S6 = F Z in FP64,
     // S6 inverted on the device
@@ -580,7 +599,9 @@ void mixed_build_swimmers(const std::vector<sqbem_swimmer*>& sw, const MixedCtx&
         }
         LAUNCH(invert6_kernel, 1, INV6_MAX, 0, cx.st, a);
     }
+    lap("Z, S6");
     check_ctx(cx, "mixed Schur inverse");
+    lap("S6 wait");
 }
 
 // ---------------------------------------------------------------- refinement

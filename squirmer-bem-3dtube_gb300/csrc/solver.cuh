@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <vector>
 
 #include "assemble.cuh"
@@ -15,15 +16,20 @@ namespace sqbem {
 
 // A CUDA stream owned by a handle, or borrowed from the caller (batched calls
 // run every handle on the batch stream).
+// A stream of its own, created at first use, or one borrowed from the caller
+// (batched paths hand every member the group's stream, and creating a stream
+// per member only to drop it cost tens of microseconds each).
 struct Stream {
-    cudaStream_t s = nullptr;
+    mutable cudaStream_t s = nullptr;
+    mutable std::once_flag once;
     bool owned = true;
-    Stream();
+    Stream() = default;
     ~Stream();
     Stream(const Stream&) = delete;
     Stream& operator=(const Stream&) = delete;
     void borrow(cudaStream_t other);
-    operator cudaStream_t() const { return s; }
+    cudaStream_t get() const;
+    operator cudaStream_t() const { return get(); }
 };
 
 // Panels of one mesh on the device: records + centroids (targets).

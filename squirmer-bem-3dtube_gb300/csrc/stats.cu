@@ -1,6 +1,7 @@
 // stats.cu -- transfer counters and opt-in per-kernel-class event timing.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -19,6 +20,7 @@ namespace {
 constexpr int MAX_COUNTS = 8;
 struct Pending {
     cudaEvent_t a = nullptr, b = nullptr;
+    cudaStream_t st = nullptr;
     std::string cls, note;
     double flops = 0, bytes = 0;
     const int* counts = nullptr;  // pinned host counters, read at collection
@@ -39,8 +41,12 @@ std::vector<Pending> g_pending;
 std::map<std::string, Agg> g_agg;
 std::vector<cudaEvent_t> g_free;  // recorded-and-collected events, reused
 // Per-launch log (profiling aid): with kernel stats enabled and SQBEM_KSTATS_LOG
-// naming a file, every timed launch appends "class microseconds flops bytes note".
+// naming a file, every timed launch appends "class microseconds flops bytes note
+// @start,end,stream": start and end in microseconds after the event recorded
+// when the log was opened, and the launching stream, so that a run on several
+// streams can be laid out as a timeline.
 FILE* g_log = nullptr;
+cudaEvent_t g_base = nullptr;
 thread_local std::string t_note;
 
 cudaEvent_t take_event() {
@@ -66,9 +72,16 @@ void collect_locked() {
                 g.seconds += ms * 1e-3;
                 g.flops += p.flops;
                 g.bytes += p.bytes;
-                if (g_log)
-                    std::fprintf(g_log, "%s %.3f %.6g %.6g %s\n", p.cls.c_str(), ms * 1e3, p.flops, p.bytes,
-                                 p.note.c_str());
+                if (g_log) {
+                    float t0 = 0, t1 = 0;
+                    if (g_base) {
+                        cudaEventElapsedTime(&t0, g_base, p.a);
+                        cudaEventElapsedTime(&t1, g_base, p.b);
+                    }
+                    std::fprintf(g_log, "%s %.3f %.6g %.6g %s @%.3f,%.3f,%llx\n", p.cls.c_str(), ms * 1e3, p.flops,
+                                 p.bytes, p.note.c_str(), t0 * 1e3, t1 * 1e3,
+                                 (unsigned long long)(uintptr_t)p.st);
+                }
             }
         }
         if (p.a) g_free.push_back(p.a);
@@ -85,6 +98,7 @@ int kstat_begin(cudaStream_t st) {
     Pending p;
     p.a = take_event();
     p.b = take_event();
+    p.st = st;
     CUDA_CHECK(cudaEventRecord(p.a, st));
     g_pending.push_back(p);
     return (int)g_pending.size() - 1;
@@ -209,7 +223,12 @@ extern "C" int sqbem_kernel_stats_enable(int on) {
             g_log = nullptr;
         }
         const char* path = std::getenv("SQBEM_KSTATS_LOG");
-        if (on && path && *path) g_log = std::fopen(path, "a");
+        if (on && path && *path) {
+            g_log = std::fopen(path, "a");
+            if (!g_base) CUDA_CHECK(cudaEventCreate(&g_base));
+            CUDA_CHECK(cudaEventRecord(g_base, 0));
+            CUDA_CHECK(cudaEventSynchronize(g_base));
+        }
         g_on.store(on != 0);
     });
 }

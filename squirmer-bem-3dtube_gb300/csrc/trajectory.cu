@@ -13,8 +13,10 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -92,6 +94,16 @@ public:
     };
 
     void solve_group(const std::vector<State>& ys, size_t c0, size_t G, bool keep, Group& gr, cudaStream_t st) {
+        // host time per phase on stderr when SQBEM_HOST_TIMING is set (profiling aid)
+        static const bool timing = std::getenv("SQBEM_HOST_TIMING") != nullptr;
+        auto tp = std::chrono::steady_clock::now();
+        auto lap = [&](const char* what) {
+            if (!timing) return;
+            const auto now = std::chrono::steady_clock::now();
+            std::fprintf(stderr, "ensemble group %zu (%zu swimmers) %-8s %.2f ms\n", c0, G, what,
+                         std::chrono::duration<double, std::milli>(now - tp).count());
+            tp = now;
+        };
         gr.sw.resize(G);
         gr.slips.resize(G);
         gr.modes.resize(G);
@@ -120,6 +132,7 @@ public:
                 gr.slips[g].insert(gr.slips[g].end(), u2.begin(), u2.end());
             }
         }
+        lap("geometry");
         if (prec_ == SQBEM_MIXED) {
             std::vector<sqbem_swimmer*> sp;
             for (auto& s : gr.sw) sp.push_back(s.get());
@@ -127,6 +140,7 @@ public:
             flags.zero();
             MixedCtx cx{st, flags.get(), flags.get() + 1};
             mixed_build_swimmers(sp, cx, share_);
+            lap("build");
             // the slip modes on the device (slip_modes_group), solved in place
             std::vector<DevBuf<double>> din(G);
             gr.dx.clear();
@@ -163,6 +177,7 @@ public:
                 count_d2h(12 * sizeof(double));
             }
             CUDA_CHECK(cudaStreamSynchronize(st));
+            lap("solve");
             for (size_t g = 0; g < G; ++g) {
                 const double* wg = w.data() + 12 * g;
                 Modes& m = gr.modes[g];
