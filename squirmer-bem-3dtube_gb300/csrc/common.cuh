@@ -6,8 +6,10 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <map>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "sqbem.h"
 
@@ -106,19 +108,79 @@ int guarded(F&& f) {
 cudaMemPool_t device_pool();
 void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st);
 
-// Owning device allocation (stream-ordered, from device_pool()).
+// Idle device blocks of one stream.  The stream-ordered allocator serialises
+// its calls across host threads behind one driver lock: on GB300's Grace host a
+// malloc/free pair took 0.6 us on one thread and 27 us per thread on six, and
+// the six concurrent workers of a 48-swimmer ensemble group spent 51-54 of
+// their 88 ms in it.  So a worker allocates through the cache of its slot
+// (below): a block freed on the slot's stream goes back to the cache, and a
+// later allocation on the same stream of the same size class takes it -- safe
+// in stream order, as the allocator's own reuse is -- with no driver call.
+// Size classes are 1/8 octave apart (at most 12.5% over the request).
+class StreamCache {
+public:
+    explicit StreamCache(cudaStream_t s) : s_(s) {}
+    StreamCache(const StreamCache&) = delete;
+    StreamCache& operator=(const StreamCache&) = delete;
+    cudaStream_t stream() const { return s_; }
+    void* take(size_t bytes);          // a block of the request's class, or null if the pool is out of memory
+    void give(void* p, size_t bytes);  // a block that take() returned, now idle
+    void trim_to(size_t keep);         // idle blocks back to the pool until at most keep bytes stay
+    size_t held() const { return held_; }
+
+private:
+    cudaStream_t s_;
+    std::map<size_t, std::vector<void*>> idle_;
+    size_t held_ = 0;
+};
+
+// Worker slot k of the current device: a stream and its block cache that last
+// for the process, so that successive batched calls (an ensemble's RK stages,
+// repeated sweeps) reuse each other's blocks.  The lease installs the cache for
+// the calling thread; a slot already leased (a concurrent call from another
+// host thread) leaves this lease with a stream of its own and no cache.
+// sqbem_trim_pool() empties the caches.
+class WorkerLease {
+public:
+    explicit WorkerLease(int k);
+    ~WorkerLease();
+    WorkerLease(const WorkerLease&) = delete;
+    WorkerLease& operator=(const WorkerLease&) = delete;
+    cudaStream_t stream() const { return st_; }
+    void end_task();  // after a task: the slot's idle blocks trimmed to its share
+
+private:
+    int dev_ = 0, k_ = -1;
+    cudaStream_t st_ = nullptr;
+    bool own_stream_ = false;
+    StreamCache* prev_ = nullptr;
+};
+void trim_worker_caches();
+
+// Device allocation on stream s: from the calling thread's slot cache when it
+// serves s (*cached set), else from the pool.  Fails with SQBEM_ERR_ALLOC.
+void* dev_alloc(size_t bytes, cudaStream_t s, bool* cached);
+void dev_free(void* p, size_t bytes, cudaStream_t s, bool cached);
+
+// Owning device allocation (stream-ordered, from device_pool() or a worker's
+// StreamCache).
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;
     cudaStream_t st = nullptr;
+    bool cached = false;
     DevBuf() = default;
     DevBuf(size_t count, cudaStream_t s) { alloc(count, s); }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), st(o.st) { o.p = nullptr; o.n = 0; }
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), st(o.st), cached(o.cached) { o.p = nullptr; o.n = 0; }
     DevBuf& operator=(DevBuf&& o) noexcept {
-        if (this != &o) { release(); p = o.p; n = o.n; st = o.st; o.p = nullptr; o.n = 0; }
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; st = o.st; cached = o.cached;
+            o.p = nullptr; o.n = 0;
+        }
         return *this;
     }
     ~DevBuf() { release(); }
@@ -127,21 +189,16 @@ struct DevBuf {
         st = s;
         n = count;
         if (count == 0) return;
-        cudaError_t e = cudaMallocFromPoolAsync((void**)&p, count * sizeof(T), device_pool(), s);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            (void)cudaGetLastError();
-            fail(SQBEM_ERR_ALLOC, "device allocation of %zu bytes failed: %s", count * sizeof(T),
-                 cudaGetErrorString(e));
-        }
+        p = static_cast<T*>(dev_alloc(count * sizeof(T), s, &cached));
     }
     void zero() {
         if (n) CUDA_CHECK(cudaMemsetAsync(p, 0, n * sizeof(T), st));
     }
     void release() {
-        if (p) cudaFreeAsync(p, st);
+        if (p) dev_free(p, n * sizeof(T), st, cached);
         p = nullptr;
         n = 0;
+        cached = false;
     }
     void upload(const T* h, size_t count) { upload_bytes(p, h, count * sizeof(T), st); }
     void download(T* h, size_t count) const {

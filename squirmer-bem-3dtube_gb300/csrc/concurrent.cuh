@@ -78,18 +78,20 @@ void run_concurrent(size_t ntasks, const std::vector<double>& task_bytes, cudaSt
     std::atomic<bool> failed{false};
     std::exception_ptr first_error;
     std::mutex emu;
-    auto worker = [&]() {
+    auto worker = [&](int slot) {
         try {
             CUDA_CHECK(cudaSetDevice(dev));
-            Stream ws;
+            WorkerLease lease(slot);  // the slot's stream and block cache
+            const cudaStream_t ws = lease.stream();
             CUDA_CHECK(cudaStreamWaitEvent(ws, start, 0));
             for (;;) {
                 const size_t k = next.fetch_add(1);
                 if (k >= ntasks || failed.load()) break;
                 budget.acquire(task_bytes[k]);
                 try {
-                    work(k, (cudaStream_t)ws);
-                    CUDA_CHECK(cudaStreamSynchronize(ws));  // its memory is back in the pool
+                    work(k, ws);
+                    CUDA_CHECK(cudaStreamSynchronize(ws));
+                    lease.end_task();
                 } catch (...) {
                     budget.release(task_bytes[k]);
                     throw;
@@ -108,10 +110,10 @@ void run_concurrent(size_t ntasks, const std::vector<double>& task_bytes, cudaSt
         }
     };
     if (W <= 1) {
-        worker();
+        worker(0);
     } else {
         std::vector<std::thread> th;
-        for (int w = 0; w < W; ++w) th.emplace_back(worker);
+        for (int w = 0; w < W; ++w) th.emplace_back(worker, w);
         for (auto& t : th) t.join();
     }
     cudaEventDestroy(start);

@@ -3,7 +3,9 @@
 // Device buffers come from one stream-ordered pool per device that keeps freed
 // memory (release threshold = max): the default pool returns it to the CUDA driver
 // at every synchronisation, and the next large allocation then has to map
-// fresh pages while the GPU waits.  sqbem_trim_pool() gives the cached memory
+// fresh pages while the GPU waits.  The concurrent workers allocate through the
+// block caches of persistent worker slots (WorkerLease, StreamCache in
+// common.cuh) in front of that pool.  sqbem_trim_pool() gives the cached memory
 // back.
 //
 // A host-to-device copy from pageable memory may wait for its stream to drain
@@ -18,6 +20,7 @@
 #include <atomic>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 
 #include "common.cuh"
@@ -102,6 +105,155 @@ cudaMemPool_t device_pool() {
     return g_pools[dev];
 }
 
+// ---------------------------------------------------------------- allocation
+namespace {
+thread_local StreamCache* t_cache = nullptr;
+
+// 1/8-octave size classes: a power of two, or the next multiple of an eighth of
+// the power of two below (256 bytes at least)
+size_t size_class(size_t b) {
+    if (b <= 256) return 256;
+    const int e = 63 - __builtin_clzll((unsigned long long)b);
+    if (b == (size_t(1) << e)) return b;
+    const size_t step = size_t(1) << (e - 3 > 8 ? e - 3 : 8);
+    return (b + step - 1) / step * step;
+}
+
+void* pool_alloc(size_t bytes, cudaStream_t s) {
+    void* p = nullptr;
+    const cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, device_pool(), s);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+// the worker slots: taken through busy (compare-exchange, so that a nested
+// lease on the same thread simply finds the slot taken)
+constexpr int MAX_SLOTS = 8;
+struct WorkerSlot {
+    std::atomic<bool> busy{false};
+    cudaStream_t st = nullptr;
+    std::unique_ptr<StreamCache> cache;
+};
+WorkerSlot g_wslots[MAX_DEV][MAX_SLOTS];
+size_t g_slot_share[MAX_DEV];  // idle bytes a slot keeps between tasks: 1/32 of the device's memory
+std::once_flag g_share_once[MAX_DEV];
+
+bool try_take(WorkerSlot& s) {
+    bool expect = false;
+    return s.busy.compare_exchange_strong(expect, true, std::memory_order_acquire);
+}
+}  // namespace
+
+void* StreamCache::take(size_t bytes) {
+    const size_t cls = size_class(bytes);
+    auto it = idle_.find(cls);
+    if (it != idle_.end() && !it->second.empty()) {
+        void* p = it->second.back();
+        it->second.pop_back();
+        held_ -= cls;
+        return p;
+    }
+    void* p = pool_alloc(cls, s_);
+    if (!p && held_ > 0) {  // the idle blocks of other classes go back first
+        trim_to(0);
+        p = pool_alloc(cls, s_);
+    }
+    return p;
+}
+
+void StreamCache::give(void* p, size_t bytes) {
+    const size_t cls = size_class(bytes);
+    idle_[cls].push_back(p);
+    held_ += cls;
+}
+
+void StreamCache::trim_to(size_t keep) {
+    for (auto it = idle_.rbegin(); it != idle_.rend() && held_ > keep; ++it)
+        while (!it->second.empty() && held_ > keep) {
+            cudaFreeAsync(it->second.back(), s_);
+            it->second.pop_back();
+            held_ -= it->first;
+        }
+}
+
+WorkerLease::WorkerLease(int k) {
+    CUDA_CHECK(cudaGetDevice(&dev_));
+    prev_ = t_cache;
+    if (dev_ >= 0 && dev_ < MAX_DEV && k >= 0 && k < MAX_SLOTS && try_take(g_wslots[dev_][k])) {
+        WorkerSlot& s = g_wslots[dev_][k];
+        if (!s.st) {
+            const cudaError_t e = cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) {
+                s.st = nullptr;
+                s.busy.store(false, std::memory_order_release);
+                CUDA_CHECK(e);
+            }
+            s.cache = std::make_unique<StreamCache>(s.st);
+        }
+        std::call_once(g_share_once[dev_], [this] {
+            size_t fr = 0, tot = 0;
+            CUDA_CHECK(cudaMemGetInfo(&fr, &tot));
+            g_slot_share[dev_] = tot / 32;
+        });
+        k_ = k;
+        st_ = s.st;
+        t_cache = s.cache.get();
+    } else {
+        CUDA_CHECK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        own_stream_ = true;
+        t_cache = nullptr;
+    }
+}
+
+WorkerLease::~WorkerLease() {
+    t_cache = prev_;
+    if (k_ >= 0) {
+        g_wslots[dev_][k_].busy.store(false, std::memory_order_release);
+    } else if (own_stream_) {
+        cudaStreamSynchronize(st_);
+        cudaStreamDestroy(st_);
+    }
+}
+
+void WorkerLease::end_task() {
+    if (k_ >= 0) g_wslots[dev_][k_].cache->trim_to(g_slot_share[dev_]);
+}
+
+void trim_worker_caches() {
+    for (auto& dev : g_wslots)
+        for (WorkerSlot& s : dev)
+            if (try_take(s)) {
+                if (s.cache) {
+                    s.cache->trim_to(0);
+                    cudaStreamSynchronize(s.st);
+                }
+                s.busy.store(false, std::memory_order_release);
+            }
+}
+
+void* dev_alloc(size_t bytes, cudaStream_t s, bool* cached) {
+    StreamCache* c = t_cache;
+    void* p = nullptr;
+    if (c && c->stream() == s) {
+        p = c->take(bytes);
+        *cached = true;
+    } else {
+        p = pool_alloc(bytes, s);
+        *cached = false;
+    }
+    if (!p) fail(SQBEM_ERR_ALLOC, "device allocation of %zu bytes failed", bytes);
+    return p;
+}
+
+void dev_free(void* p, size_t bytes, cudaStream_t s, bool cached) {
+    StreamCache* c = t_cache;
+    if (cached && c && c->stream() == s) c->give(p, bytes);
+    else cudaFreeAsync(p, s);
+}
+
 void upload_bytes(void* dst, const void* src, size_t bytes, cudaStream_t st) {
     count_h2d(bytes);
     if (bytes == 0) return;
@@ -154,6 +306,7 @@ using namespace sqbem;
 extern "C" int sqbem_trim_pool(void) {
     return guarded([&] {
         require_device();
+        trim_worker_caches();
         CUDA_CHECK(cudaDeviceSynchronize());
         CUDA_CHECK(cudaMemPoolTrimTo(device_pool(), 0));
     });
