@@ -240,10 +240,14 @@ void mixed_build_tubes(const std::vector<sqbem_tube*>& tubes, const MixedCtx& cx
         }
         fourier_build(fts, sp, t0p, cx);
         check_ctx(cx, "mixed tube (Fourier blocks)");
-        if (explicit_inverse) {
-            // a tube shared by many swimmers: T^{-1} by solving the identity through
-            // the blocks, FP32 (for the refinement's products) and split row-major
-            // (the left operand of every swimmer's Y = T^{-1} [B | Ct])
+        // A tube shared by many swimmers could also keep T^{-1} (solving the identity
+        // through the blocks: FP32 for the refinement's products, split row-major as
+        // the left operand of every swimmer's Y = T^{-1} [B | Ct]).  The per-swimmer
+        // Fourier solves are cheaper than those dense products (K = 3 Nt): on the
+        // 256-swimmer ensemble 4250 against 3871 solves/s, so the dense inverse is
+        // formed only when SQBEM_FOURIER_EXPLICIT=1 asks for it.
+        const char* fe = std::getenv("SQBEM_FOURIER_EXPLICIT");
+        if (explicit_inverse && fe && std::atoi(fe) != 0) {
             for (size_t k = 0; k < G; ++k) {
                 MixedTube& M = tubes[k]->mt;
                 const size_t nn = (size_t)M.ntp * M.ntp;
