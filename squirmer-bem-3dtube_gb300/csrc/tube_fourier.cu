@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -397,95 +398,54 @@ __global__ void __launch_bounds__(64) idft_kernel(const __grid_constant__ DftArg
     }
 }
 
-// The same transforms and block builder for a sector count known at compile
-// time: every loop over sectors and frequencies unrolled, so the twiddle index
-// (f s mod NTH) is a constant and the twiddles (kernel parameters) are constant
-// operands of the multiply-adds; each CTA of the transforms takes FT_JC columns.
-// Persistent CTAs over the columns of X: the tube's panel map is staged in shared
-// memory once, and the columns go through two shared-memory buffers -- the next
-// column's copy (cp.async) runs while the current one is transformed, so the
-// sector loop reads shared memory only.  FP64 input (the refinement's few
-// columns) is staged synchronously.  Dynamic shared memory: nb NTH map entries +
-// 2 x 3 nb NTH column values.
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all_but(int n) {
-    if (n) asm volatile("cp.async.wait_group 1;" ::: "memory");
-    else asm volatile("cp.async.wait_group 0;" ::: "memory");
-}
-
+// Both transforms with a thread per representative a and column (blockIdx.x;
+// job: blockIdx.y), all three components of its rows in the thread: the rotation
+// R_s needs no exchange between lanes, every panel load and twiddle serves three
+// rows, and with the sector and frequency loops unrolled the twiddles are
+// constant operands of the multiply-adds.
 template <int NTH, class TI>
-__global__ void __launch_bounds__(192, 3) fdft_nth(const __grid_constant__ DftArgs args) {
+__global__ void __launch_bounds__(64) fdft_rep(const __grid_constant__ DftArgs args) {
     constexpr int NF = NTH / 2 + 1;
-    constexpr bool ASYNC = sizeof(TI) == sizeof(float);
-    extern __shared__ float fsm[];
     const DftJob& J = args.j[blockIdx.y];
-    int j = blockIdx.x;
+    const int j = blockIdx.x;
     if (j >= J.nc) return;
-    const int n3 = 3 * J.nb, nt = n3 * NTH;
-    int* pan = reinterpret_cast<int*>(fsm);  // nb x NTH panel map
-    float* buf[2] = {fsm + J.nb * NTH, fsm + J.nb * NTH + nt};
-    const TI* X = reinterpret_cast<const TI*>(J.x);
-    for (int e = threadIdx.x; e < J.nb * NTH; e += blockDim.x) pan[e] = J.panel[e];
-    if (ASYNC) {
-        const float* x = reinterpret_cast<const float*>(X) + (long long)j * J.ldx;
-        for (int e = threadIdx.x; e < nt; e += blockDim.x) cp_async4(buf[0] + e, x + e);
-        cp_async_commit();
-    }
+    const int n3 = 3 * J.nb;
+    const TI* x = reinterpret_cast<const TI*>(J.x) + (long long)j * J.ldx;
     const float scale = 1.f / (float)NTH;
-    for (int it = 0;; ++it) {
-        float* xs = buf[it & 1];
-        const int jn = j + gridDim.x;
-        if (ASYNC) {
-            if (jn < J.nc) {
-                const float* x = reinterpret_cast<const float*>(X) + (long long)jn * J.ldx;
-                float* nx = buf[(it + 1) & 1];
-                for (int e = threadIdx.x; e < nt; e += blockDim.x) cp_async4(nx + e, x + e);
-                cp_async_commit();
-            }
-            cp_async_wait_all_but(jn < J.nc ? 1 : 0);
-        } else {
-            const TI* x = X + (long long)j * J.ldx;
-            for (int e = threadIdx.x; e < nt; e += blockDim.x) xs[e] = (float)x[e];
+    for (int a = threadIdx.x; a < J.nb; a += blockDim.x) {
+        const int* pa = J.panel + a * NTH;
+        float v[3][NTH];  // R_s^T x_{panel(a, s)}
+#pragma unroll
+        for (int s = 0; s < NTH; ++s) {
+            const TI* xp = x + 3LL * __ldg(pa + s);
+            const float x0 = (float)__ldg(xp), x1 = (float)__ldg(xp + 1);
+            const float c = args.tw[s].x, sn = args.tw[s].y;
+            v[0][s] = c * x0 + sn * x1;
+            v[1][s] = -sn * x0 + c * x1;
+            v[2][s] = (float)__ldg(xp + 2);
         }
-        __syncthreads();
-        for (int r = threadIdx.x; r < n3; r += blockDim.x) {
-            const int a = r / 3, al = r - 3 * a;
-            const int* pa = pan + a * NTH;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int r = 3 * a + c;
             float re[NF], im[NF];
 #pragma unroll
-            for (int f = 0; f < NF; ++f) re[f] = im[f] = 0.f;
-            // (R_s^T x_p)_al of sector s
-            auto vsec = [&](int s) {
-                const float* xp = xs + 3 * pa[s];
-                if (al == 2) return xp[2];
-                const float c = args.tw[s].x, sn = args.tw[s].y;
-                return al == 0 ? c * xp[0] + sn * xp[1] : -sn * xp[0] + c * xp[1];
-            };
-            // real input: sectors s and NTH - s share cos(2 pi f s / NTH) and have
-            // opposite sines, so they enter as their sum and difference
-            {
-                const float v0 = vsec(0);
-#pragma unroll
-                for (int f = 0; f < NF; ++f) re[f] = v0;
+            for (int f = 0; f < NF; ++f) {
+                re[f] = v[c][0];
+                im[f] = 0.f;
             }
+            // sectors s and NTH - s: shared cosines, opposite sines
 #pragma unroll
             for (int s = 1; 2 * s < NTH; ++s) {
-                const float va = vsec(s), vb = vsec(NTH - s);
-                const float sum = va + vb, dif = va - vb;
+                const float sum = v[c][s] + v[c][NTH - s], dif = v[c][s] - v[c][NTH - s];
 #pragma unroll
                 for (int f = 0; f < NF; ++f) {
                     re[f] += sum * args.tw[(f * s) % NTH].x;
                     im[f] -= dif * args.tw[(f * s) % NTH].y;
                 }
             }
-            if ((NTH & 1) == 0) {  // sector NTH / 2: w^{-f NTH/2} = (-1)^f
-                const float vh = vsec(NTH / 2);
+            if ((NTH & 1) == 0) {
 #pragma unroll
-                for (int f = 0; f < NF; ++f) re[f] += (f & 1) ? -vh : vh;
+                for (int f = 0; f < NF; ++f) re[f] += (f & 1) ? -v[c][NTH / 2] : v[c][NTH / 2];
             }
 #pragma unroll
             for (int f = 0; f < NF; ++f) {
@@ -498,9 +458,6 @@ __global__ void __launch_bounds__(192, 3) fdft_nth(const __grid_constant__ DftAr
                 J.l[o + n3 + r] = __float2bfloat16_rn(vi - __bfloat162float(hi));
             }
         }
-        __syncthreads();  // the buffer just read is the next prefetch's target
-        j = jn;
-        if (j >= J.nc) break;
     }
 }
 
@@ -629,14 +586,6 @@ void set_smem_limits() {
     std::call_once(once, [] {
         CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
         CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
-        // the forward transform: the panel map and two columns, 7 nb n_theta floats (<= 7 * 256 / 3 * 36 * 4 B)
-        const int fd = 7 * (FT_MAX_ORDER / 3) * FT_MAX_SECTORS * 4;
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<24, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<30, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
-        CUDA_CHECK(cudaFuncSetAttribute(fdft_nth<36, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, fd));
     });
 }
 
@@ -803,23 +752,17 @@ void fourier_solve(const std::vector<FourierJob>& jobs, const MixedCtx& cx) {
         const int nth = jobs[i0].ft->nth;
         set_tw(a, nth);
         const double by = dft_bytes(i0, a.n, true);
-        // persistent CTAs: about 8 per SM over the launch's jobs
-        const int per_job = std::max(1, std::min(maxnc, ceil_div(8 * 152, a.n)));
-        const dim3 gs(per_job, a.n);
-        int nbmax = 0;
-        for (int q = 0; q < a.n; ++q) nbmax = std::max(nbmax, a.j[q].nb);
-        const size_t sm = sizeof(float) * (size_t)nbmax * nth * 7;  // map + two columns of 3 nb nth values
-        set_smem_limits();
+        const dim3 gd(maxnc, a.n);
         if (in64) {
-            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, double>), gs, 192, sm, cx.st, a);
-            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, double>), gs, 192, sm, cx.st, a);
-            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<36, double>), gs, 192, sm, cx.st, a);
-            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<double>, dim3(maxnc, a.n), 192, 0, cx.st, a);
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<24, double>), gd, 64, 0, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<30, double>), gd, 64, 0, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<36, double>), gd, 64, 0, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<double>, gd, 192, 0, cx.st, a);
         } else {
-            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<24, float>), gs, 192, sm, cx.st, a);
-            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<30, float>), gs, 192, sm, cx.st, a);
-            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_nth<36, float>), gs, 192, sm, cx.st, a);
-            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<float>, dim3(maxnc, a.n), 192, 0, cx.st, a);
+            if (nth == 24) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<24, float>), gd, 64, 0, cx.st, a);
+            else if (nth == 30) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<30, float>), gd, 64, 0, cx.st, a);
+            else if (nth == 36) TIMED_LAUNCH("fourier_dft", 0.0, by, (fdft_rep<36, float>), gd, 64, 0, cx.st, a);
+            else TIMED_LAUNCH("fourier_dft", 0.0, by, fdft_kernel<float>, gd, 192, 0, cx.st, a);
         }
     }
     // one GEMM of order 2 n3 per job and frequency: Y^_f = inv(C^_f) X^_f in real form
