@@ -385,13 +385,13 @@ def run_aux(args, rank, ws):
         u, fsecs = sqbem.ensemble_field(states[:, -1, :], alpha, P, 25, 25, 41, 7.0, precision=prec)
         pts = int(np.sum(~np.isnan(u[..., 0])))
         line = {"metric": "trajectory-ensemble BEM solves/sec (each solve: swimmer re-assembly, Schur and the two "
-                          "slip modes against the shared tube inverse)", "value": solves / gpu_s, "unit": "solves/s",
+                          "slip modes against the shared tube's Fourier blocks)", "value": solves / gpu_s, "unit": "solves/s",
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * gpu_s / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32/bf16x3+f64" if prec == sqbem.MIXED else "f64", "data": "synthetic",
                 "config": {"workload": "ensemble (%d swimmers, a/R = %.1f, level %d, n_theta = %d, RK4 dt = %g, "
-                                       "%d steps per call; each timed call assembles and factors the tube once "
-                                       "(%d factorizations in the timed region), the sphere-sphere blocks once)"
+                                       "%d steps per call; each timed call assembles the tube and inverts its Fourier blocks "
+                                       "once (%d tube builds in the timed region), the sphere-sphere blocks once)"
                                        % (len(w), w[0]["a_over_R"], w[0]["sphere_level"], w[0]["n_theta"], w[0]["dt"],
                                           rk_steps, tube_builds)},
                 "e2e": {"value": solves / wall, "unit": "solves/s"},
