@@ -206,183 +206,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gj_k
         }
 }
 
-// The same inversion blocked by panels of GJ_PANEL columns.  The GJ_PANEL steps
-// of a panel act on every other column as one linear map: the panel's row
-// exchanges, then col <- zero_K(col) + G_K col_K, where K are the panel's rows
-// and G_K is what the panel's own columns become when the steps are applied to
-// them alone (the in-place rule turns each pivot column into a column of the
-// inverse).  So the CTA owning a panel factors it by itself (a barrier per
-// step inside one CTA), writes the factored panel and its pivot rows into every
-// CTA's shared memory (double-buffered), and after one cluster barrier every
-// CTA applies the exchanges and the rank-GJ_PANEL update to its other columns:
-// n / GJ_PANEL cluster barriers instead of n, and the bulk of the work is
-// multiply-adds with a panel column per lane.  The row exchanges are undone as
-// column exchanges when the columns are written back.  A zero pivot sets bit 1
-// of *flag.
-constexpr int GJ_PANEL = 8;
-
-size_t gjb_smem(int n, int cl) {
-    const int w = (n + cl - 1) / cl;
-    return (size_t)n * w * sizeof(float2) + (2 * (size_t)n * GJ_PANEL + n) * sizeof(float2) + (2 + 2 * n) * sizeof(int);
-}
-
-template <int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(GJ_THREADS, 1) gjb_kernel(const __grid_constant__ GjArgs args) {
-    cg::cluster_group cl = cg::this_cluster();
-    extern __shared__ float2 gsm[];
-    const int n = args.n, w = args.w;
-    const int rank = (int)cl.block_rank();
-    const int blk = blockIdx.x / CL;
-    float2* A = gsm;                                     // n x w, column-major, leading dimension n
-    float2* pan = gsm + (size_t)n * w;                   // 2 x n x GJ_PANEL: the factored panel (double-buffered)
-    float2* mk = pan + 2 * (size_t)n * GJ_PANEL;         // n: multipliers of a panel step
-    int* meta = reinterpret_cast<int*>(mk + n);          // [2]: zero pivot in the panel, per buffer
-    int* piv = meta + 2;                                 // n: pivot row of every step
-    int* pos = piv + n;                                  // n: output column of every stored column
-    const int c0 = rank * w, wl = max(0, min(w, n - c0));
-    float2* C = blk < args.nblk ? args.C[blk] : nullptr;
-    if (C)
-        for (int e = threadIdx.x; e < n * wl; e += blockDim.x) A[e] = C[(long long)c0 * n + e];
-    cl.sync();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    bool bad = false;
-    for (int k0 = 0, q = 0; k0 < n; ++q) {
-        const int owner = k0 / w;
-        const int bk = min(GJ_PANEL, min(n, (owner + 1) * w) - k0);  // panels never straddle two CTAs
-        const int buf = q & 1;
-        if (rank == owner) {
-            float2* Ak = A + (size_t)(k0 - c0) * n;  // the panel's columns
-            int zero = 0;
-            for (int t = 0; t < bk; ++t) {
-                const int k = k0 + t;
-                const float2* ck = Ak + (size_t)t * n;
-                if (warp == 0) {
-                    float best = -1.f;
-                    int bi = k;
-                    for (int i = k + lane; i < n; i += 32) {
-                        const float2 v = ck[i];
-                        const float m = v.x * v.x + v.y * v.y;
-                        if (m > best) { best = m; bi = i; }
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-                    }
-                    if (lane == 0) piv[k] = best > 0.f ? bi : -1;
-                }
-                __syncthreads();
-                const int p = piv[k];
-                if (p < 0) {  // the same in every thread of the CTA
-                    zero = 1;
-                    break;
-                }
-                const float2 pv = ck[p];
-                const float s2 = 1.f / (pv.x * pv.x + pv.y * pv.y);
-                const float2 d = make_float2(pv.x * s2, -pv.y * s2);  // 1 / pivot
-                // the multipliers after the exchange, row k's set to zero
-                for (int i = threadIdx.x; i < n; i += blockDim.x) mk[i] = i == k ? make_float2(0.f, 0.f) : ck[i == p ? k : i];
-                __syncthreads();
-                // exchange rows k and p of the panel's columns and scale the new row k
-                for (int jl = threadIdx.x; jl < bk; jl += blockDim.x) {
-                    float2* col = Ak + (size_t)jl * n;
-                    const float2 vk = col[k], vp = col[p];
-                    col[p] = vk;
-                    col[k] = jl == t ? d : cmul(vp, d);
-                }
-                __syncthreads();
-                // eliminate within the panel; its column t becomes a column of the inverse
-                for (int e = threadIdx.x; e < n * bk; e += blockDim.x) {
-                    const int jl = e / n, i = e - jl * n;
-                    if (i == k) continue;
-                    float2* col = Ak + (size_t)jl * n;
-                    if (jl == t) {
-                        const float2 u = cmul(mk[i], d);
-                        col[i] = make_float2(-u.x, -u.y);
-                    } else {
-                        const float2 rk = col[k], m = mk[i], c = col[i];
-                        col[i] = make_float2(c.x - (m.x * rk.x - m.y * rk.y), c.y - (m.x * rk.y + m.y * rk.x));
-                    }
-                }
-                __syncthreads();
-            }
-            // the factored panel, its pivot rows and the zero flag into every CTA
-            for (int e = threadIdx.x; e < CL * n * bk; e += blockDim.x) {
-                const int qq = e / (n * bk), r = e - qq * (n * bk);
-                cl.map_shared_rank(pan, qq)[(size_t)buf * n * GJ_PANEL + r] = Ak[r];
-            }
-            for (int e = threadIdx.x; e < CL * bk; e += blockDim.x) {
-                const int qq = e / bk, t = e - qq * bk;
-                cl.map_shared_rank(piv, qq)[k0 + t] = piv[k0 + t];
-            }
-            if (threadIdx.x < CL) cl.map_shared_rank(meta, threadIdx.x)[buf] = zero;
-        }
-        cl.sync();
-        if (meta[buf]) {  // the same in every CTA of the cluster
-            bad = true;
-            break;
-        }
-        // this CTA's other columns: the panel's exchanges in order, then
-        // col <- zero_K(col) + G_K col_K
-        const float2* G = pan + (size_t)buf * n * GJ_PANEL;
-        for (int jl = warp; jl < wl; jl += nw) {
-            const int j = c0 + jl;
-            if (j >= k0 && j < k0 + bk) continue;
-            float2* col = A + (size_t)jl * n;
-            if (lane == 0)
-                for (int t = 0; t < bk; ++t) {
-                    const int k = k0 + t, p = piv[k];
-                    const float2 v = col[k];
-                    col[k] = col[p];
-                    col[p] = v;
-                }
-            __syncwarp();
-            float2 X[GJ_PANEL];
-#pragma unroll
-            for (int t = 0; t < GJ_PANEL; ++t) X[t] = t < bk ? col[k0 + t] : make_float2(0.f, 0.f);
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) {
-                float2 v = (i >= k0 && i < k0 + bk) ? make_float2(0.f, 0.f) : col[i];
-#pragma unroll
-                for (int t = 0; t < GJ_PANEL; ++t) {
-                    if (t < bk) {
-                        const float2 g = G[(size_t)t * n + i];
-                        v.x += g.x * X[t].x - g.y * X[t].y;
-                        v.y += g.x * X[t].y + g.y * X[t].x;
-                    }
-                }
-                col[i] = v;
-            }
-        }
-        __syncthreads();
-        k0 += bk;
-    }
-    if (bad) {
-        if (threadIdx.x == 0 && rank == 0) atomicOr(args.flag, 2);
-        return;
-    }
-    if (threadIdx.x == 0) {
-        // stored column cur[c] is output column c: the exchanges (k, piv[k]) in reverse order
-        int* cur = pos;
-        for (int c = 0; c < n; ++c) cur[c] = c;
-        for (int k = n - 1; k >= 0; --k) {
-            const int p = piv[k];
-            if (p != k) { const int t = cur[k]; cur[k] = cur[p]; cur[p] = t; }
-        }
-        int* inv = reinterpret_cast<int*>(pan);  // the panel buffers are no longer needed
-        for (int c = 0; c < n; ++c) inv[cur[c]] = c;
-        for (int c = 0; c < n; ++c) pos[c] = inv[c];
-    }
-    __syncthreads();
-    if (C)
-        for (int jl = warp; jl < wl; jl += nw) {
-            float2* dst = C + (long long)pos[c0 + jl] * n;
-            const float2* src = A + (size_t)jl * n;
-            for (int i = lane; i < n; i += 32) dst[i] = src[i];
-        }
-}
-
 // The real form [[Re, -Im], [Im, Re]] of every inverse (n x n complex,
 // column-major) as split BF16, row-major with leading dimension ldk, through
 // 32 x 32 shared-memory tiles: reads along the source columns, writes along the
@@ -737,22 +560,20 @@ __global__ void chat_nth(const __grid_constant__ ChatArgs args, const __grid_con
     for (int f = 0; f < NF; ++f) J.C[(long long)f * n3 * n3 + (long long)c * n3 + r] = make_float2(re[f], im[f]);
 }
 
+int gj_cluster(int n) {
+    // shared memory of one CTA: its columns, two pivot columns and the index
+    // arrays; two CTAs per block where they fit (measured faster than four)
+    for (int cl : {2, 4}) {
+        const int w = (n + cl - 1) / cl;
+        const size_t bytes = (size_t)n * w * sizeof(float2) + 3 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
+        if (bytes <= 220 * 1024) return cl;
+    }
+    return 0;
+}
+
 size_t gj_smem(int n, int cl) {
     const int w = (n + cl - 1) / cl;
     return (size_t)n * w * sizeof(float2) + 3 * n * sizeof(float2) + (2 + 2 * n) * sizeof(int);
-}
-
-bool gj_blocked() {
-    static const bool b = !std::getenv("SQBEM_GJ_BLOCKED") || std::atoi(std::getenv("SQBEM_GJ_BLOCKED")) != 0;
-    return b;
-}
-
-int gj_cluster(int n) {
-    // shared memory of one CTA: its columns, the pivot columns or panels and the
-    // index arrays; two CTAs per block where they fit (measured faster than four)
-    for (int cl : {2, 4})
-        if (std::max(gj_smem(n, cl), gjb_smem(n, cl)) <= 220 * 1024) return cl;
-    return 0;
 }
 
 // The dynamic shared memory limits of the kernels that need more than 48 KB, set
@@ -765,8 +586,6 @@ void set_smem_limits() {
     std::call_once(once, [] {
         CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
         CUDA_CHECK(cudaFuncSetAttribute(gj_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
-        CUDA_CHECK(cudaFuncSetAttribute(gjb_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
-        CUDA_CHECK(cudaFuncSetAttribute(gjb_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, FT_SMEM_MAX));
     });
 }
 
@@ -828,8 +647,7 @@ void fourier_build(const std::vector<FourierTube*>& fts, const std::vector<const
             else TIMED_LAUNCH("fourier_inverse", 0.0, cby, chat_kernel, cg3, 64, 0, cx.st, a);
         }
         const int cl = gj_cluster(n3);
-        const bool blocked = gj_blocked();
-        const size_t smem = blocked ? gjb_smem(n3, cl) : gj_smem(n3, cl);
+        const size_t smem = gj_smem(n3, cl);
         const int nblk_all = (int)(ids.size() * nf);
         for (int b0 = 0; b0 < nblk_all; b0 += GJ_MAXB) {
             GjArgs g;
@@ -853,13 +671,8 @@ void fourier_build(const std::vector<FourierTube*>& fts, const std::vector<const
             // credited: 8 n^3 FP32 flops per complex inversion; bytes: the block read and written
             const double gfl = 8.0 * g.nblk * (double)n3 * n3 * n3, gby = 16.0 * g.nblk * (double)n3 * n3;
             set_smem_limits();
-            if (blocked) {
-                if (cl == 2) TIMED_LAUNCH("fourier_inverse", gfl, gby, gjb_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
-                else TIMED_LAUNCH("fourier_inverse", gfl, gby, gjb_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
-            } else {
-                if (cl == 2) TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
-                else TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
-            }
+            if (cl == 2) TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<2>, 2 * g.nblk, GJ_THREADS, smem, cx.st, g);
+            else TIMED_LAUNCH("fourier_inverse", gfl, gby, gj_kernel<4>, 4 * g.nblk, GJ_THREADS, smem, cx.st, g);
             const int t = ceil_div(2 * n3, 32);
             TIMED_LAUNCH("fourier_inverse", 0.0, g.nblk * (8.0 * n3 * n3 + 16.0 * n3 * n3), realform_kernel,
                          dim3(t, t, g.nblk), dim3(32, 8), 0, cx.st, r);
