@@ -673,7 +673,20 @@ template void assemble_block<double>(const BlockJob<double>&, int, cudaStream_t,
 template void assemble_block<float>(const BlockJob<float>&, int, cudaStream_t, bool);
 
 // ---------------------------------------------------------------- row sums
-// partial[chunk][row][b] = sum over source panels p in the chunk of D(row, 3p + b)
+// partial[chunk][row][b] = sum over source panels p in the chunk of D(row, 3p + b).
+// FP64 blocks are summed in FP64.  FP32 blocks are summed in FP32 pairs: each
+// entry enters through an error-free TwoSum (the rounding error of every
+// addition kept in a second FP32 sum), so the chunk's (double)s + (double)c is
+// accurate to about 2^-48 of the sum of magnitudes -- what an FP64 sum of the
+// FP32 entries gives -- at 6 FP32 operations per entry instead of an FP64 add
+// (1/64 of the FP32 rate on GB300, which made this kernel FP64-bound).
+__device__ __forceinline__ void two_sum_f(float& s, float& c, float x) {
+    const float t = __fadd_rn(s, x);
+    const float z = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z)));
+    s = t;
+}
+
 template <class T>
 __global__ void rowsum_kernel(const T* __restrict__ D, long long rs, long long cs, int nrows, int ncolpanels,
                               int chunk, double* __restrict__ partial) {
@@ -681,15 +694,28 @@ __global__ void rowsum_kernel(const T* __restrict__ D, long long rs, long long c
     if (row >= nrows) return;
     const int c = blockIdx.y;
     const int p0 = c * chunk, p1 = min(ncolpanels, p0 + chunk);
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int p = p0; p < p1; ++p) {
-        const long long base = row * rs + 3LL * p * cs;
-        s0 += (double)D[base];
-        s1 += (double)D[base + cs];
-        s2 += (double)D[base + 2 * cs];
-    }
     double* o = partial + ((long long)c * nrows + row) * 3;
-    o[0] = s0; o[1] = s1; o[2] = s2;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        float s[3] = {0.f, 0.f, 0.f}, e[3] = {0.f, 0.f, 0.f};
+#pragma unroll 4
+        for (int p = p0; p < p1; ++p) {
+            const long long base = row * rs + 3LL * p * cs;
+            const float d0 = __ldg(D + base), d1 = __ldg(D + base + cs), d2 = __ldg(D + base + 2 * cs);
+            two_sum_f(s[0], e[0], d0);
+            two_sum_f(s[1], e[1], d1);
+            two_sum_f(s[2], e[2], d2);
+        }
+        for (int b = 0; b < 3; ++b) o[b] = (double)s[b] + (double)e[b];
+    } else {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int p = p0; p < p1; ++p) {
+            const long long base = row * rs + 3LL * p * cs;
+            s0 += (double)D[base];
+            s1 += (double)D[base + cs];
+            s2 += (double)D[base + 2 * cs];
+        }
+        o[0] = s0; o[1] = s1; o[2] = s2;
+    }
 }
 
 // Add the chunked row sums (fixed order) to out[row * 3 + b]
@@ -709,7 +735,7 @@ __global__ void rowsum_finish(const double* __restrict__ partial, int nchunk, in
 template <class T>
 void add_rowsums(const T* D, long long rs, long long cs, int nrows, int ncolpanels, double* out, cudaStream_t st) {
     if (nrows <= 0 || ncolpanels <= 0) return;
-    const int chunk = 32;
+    const int chunk = sizeof(T) == sizeof(float) ? 128 : 32;
     const int nchunk = ceil_div(ncolpanels, chunk);
     DevBuf<double> part((size_t)nchunk * nrows * 3, st);
     LAUNCH(rowsum_kernel<T>, dim3(ceil_div(nrows, 128), nchunk), 128, 0, st, D, rs, cs, nrows, ncolpanels, chunk,
