@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 
 #include "common.cuh"
@@ -135,6 +136,65 @@ __global__ void __launch_bounds__(MV_ROWS) mv_partial32(const __grid_constant__ 
 #pragma unroll
     for (int k = 0; k < R; ++k)
         if (k < r) o[k] = (double)s[k] + (double)cc[k];
+}
+
+// PLAIN with two rows per thread: one 8-byte load gives a thread rows 2t and
+// 2t + 1 of a column, so a warp reads 256 contiguous bytes per load and the
+// load count halves.  Used when every job's base address and leading
+// dimension keep those loads 8-byte aligned (checked on the host).
+template <int R>
+__global__ void __launch_bounds__(MV_ROWS) mv_plain2(const __grid_constant__ MvArgs args, double* __restrict__ part) {
+    constexpr int NB = 2 * MV_BATCH;
+    static_assert(MV_CHUNK % NB == 0 && NB % 4 == 0, "matvec chunk must be a multiple of the load batch");
+    __shared__ __align__(16) float xs[R][MV_CHUNK];
+    const int jb = blockIdx.z, c = blockIdx.y;
+    const int nchunk = args.j[jb].nchunk;
+    if (c >= nchunk) return;
+    const float* __restrict__ A = args.j[jb].j.A32;
+    const double* __restrict__ X = args.j[jb].j.x;
+    const long long lda = args.j[jb].j.lda, ldx = args.j[jb].j.ldx;
+    const int m = args.j[jb].j.m, n = args.j[jb].j.n, r = args.j[jb].j.r;
+    const long long poff = args.j[jb].part_off;
+    const int rstride = args.j[jb].rstride;
+    const int j0 = c * MV_CHUNK, nj = min(n, j0 + MV_CHUNK) - j0;
+    for (int e = threadIdx.x; e < R * MV_CHUNK; e += MV_ROWS) {
+        const int k = e / MV_CHUNK, j = e % MV_CHUNK;
+        xs[k][j] = (k < r && j < nj) ? (float)X[j0 + j + (long long)k * ldx] : 0.f;
+    }
+    __syncthreads();
+    const int row = 2 * (blockIdx.x * MV_ROWS + threadIdx.x);
+    if (row >= m) return;
+    const bool two = row + 1 < m;
+    float s0[R], s1[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) s0[k] = s1[k] = 0.f;
+    const float* a = A + row + (long long)j0 * lda;
+    for (int j = 0; j < nj; j += NB) {
+        float2 av[NB];
+#pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const float* p = a + (long long)(j + u) * lda;
+            av[u] = j + u < nj ? (two ? __ldg(reinterpret_cast<const float2*>(p)) : make_float2(__ldg(p), 0.f))
+                               : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < NB; u += 4)
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const float4 q = *reinterpret_cast<const float4*>(&xs[k][j + u]);
+                s0[k] = fmaf(av[u].x, q.x, s0[k]);     s1[k] = fmaf(av[u].y, q.x, s1[k]);
+                s0[k] = fmaf(av[u + 1].x, q.y, s0[k]); s1[k] = fmaf(av[u + 1].y, q.y, s1[k]);
+                s0[k] = fmaf(av[u + 2].x, q.z, s0[k]); s1[k] = fmaf(av[u + 2].y, q.z, s1[k]);
+                s0[k] = fmaf(av[u + 3].x, q.w, s0[k]); s1[k] = fmaf(av[u + 3].y, q.w, s1[k]);
+            }
+    }
+    double* o = part + poff + ((long long)c * m + row) * rstride;
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+        if (k < r) {
+            o[k] = (double)s0[k];
+            if (two) o[rstride + k] = (double)s1[k];
+        }
 }
 
 template <int R>
@@ -429,10 +489,17 @@ static void matvec_launches(const std::vector<MvJob>& jobs, cudaStream_t st) {
             kstat_note(note);
         }
         const bool plain = all32 && a.j[0].j.plain;
+        // two rows per thread: every base and leading dimension keeps 8-byte loads aligned
+        bool pairs_ok = true;
+        for (int k = 0; k < a.n && pairs_ok; ++k)
+            pairs_ok = a.j[k].j.A32 && ((uintptr_t)a.j[k].j.A32 % 8 == 0) && a.j[k].j.lda % 2 == 0;
         if (few) {
             const dim3 g(1, maxc, (unsigned)a.n);
             if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, mv_few<2>, g, 32 * MV_FEW_WARPS, 0, st, a, part.get());
             else TIMED_LAUNCH("matvec", 0.0, bytes, mv_few<MV_RMAX>, g, 32 * MV_FEW_WARPS, 0, st, a, part.get());
+        } else if (plain && pairs_ok && maxr <= 2) {
+            const dim3 g2(ceil_div(maxm, 2 * MV_ROWS), maxc, (unsigned)a.n);
+            TIMED_LAUNCH("matvec", 0.0, bytes, mv_plain2<2>, g2, MV_ROWS, 0, st, a, part.get());
         } else if (plain) {
             if (maxr <= 2) TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<2, true>), grid, MV_ROWS, 0, st, a, part.get());
             else TIMED_LAUNCH("matvec", 0.0, bytes, (mv_partial32<MV_RMAX, true>), grid, MV_ROWS, 0, st, a, part.get());
