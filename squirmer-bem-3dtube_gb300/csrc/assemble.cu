@@ -735,7 +735,7 @@ __global__ void rowsum_finish(const double* __restrict__ partial, int nchunk, in
 template <class T>
 void add_rowsums(const T* D, long long rs, long long cs, int nrows, int ncolpanels, double* out, cudaStream_t st) {
     if (nrows <= 0 || ncolpanels <= 0) return;
-    const int chunk = sizeof(T) == sizeof(float) ? 128 : 32;
+    const int chunk = 32;  // panels per CTA column: many CTAs, so the loads overlap
     const int nchunk = ceil_div(ncolpanels, chunk);
     DevBuf<double> part((size_t)nchunk * nrows * 3, st);
     LAUNCH(rowsum_kernel<T>, dim3(ceil_div(nrows, 128), nchunk), 128, 0, st, D, rs, cs, nrows, ncolpanels, chunk,
