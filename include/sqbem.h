@@ -88,9 +88,12 @@ int sqbem_kernel_stats(const char* cls, long long* launches, double* seconds, do
 int sqbem_kernel_stats_classes(char* buf, int cap);
 
 /* Device memory: the library allocates from its own stream-ordered pool, which
- * keeps freed memory for reuse (no re-mapping between batches).  trim_pool waits
- * for the device and returns the cached memory to the CUDA driver.  (No counterpart
- * in the reference, which has no device memory.) */
+ * keeps freed memory for reuse (no re-mapping between batches); the workers of
+ * the batched calls also keep up to 1/32 of the device's memory each in idle
+ * blocks of their own stream, reused by the next call without the driver's
+ * allocator.  trim_pool empties those caches (of workers not running), waits for
+ * the device and returns the cached memory to the CUDA driver.  (No counterpart in
+ * the reference, which has no device memory.) */
 int sqbem_trim_pool(void);
 
 /* ---------------------------------------------------------------- geometry
